@@ -1,0 +1,211 @@
+// TEST INFRASTRUCTURE ONLY - never linked into the product library.
+//
+// A minimal C++ model of the WGSL types and builtins that the reference's
+// simulation shaders use (src/engine/wgsl.ts, src/engine/f1.ts,
+// src/engine/car-model.ts:59-136).  oracle/wgsl_translate.py rewrites the
+// shader text itself into C++ that compiles against this header, so the
+// reference's own arithmetic runs on the CPU without WebGPU.
+//
+// Semantics follow the WGSL specification's definitions:
+//   min(a,b) = b < a ? b : a          max(a,b) = a < b ? b : a
+//   clamp(e,lo,hi) = min(max(e,lo),hi)
+//   mix(a,b,t) = a*(1-t) + b*t        smoothstep: t=clamp((x-lo)/(hi-lo),0,1); t*t*(3-2t)
+//   length(v) = sqrt(dot(v,v)), dot summed x,y,z,w in order
+//   round = ties to even               f32->i32/u32 truncate toward zero, clamped
+// sin, cos and atan are implementation-defined in WGSL; they resolve to the
+// project's own functions (wt_fmath.h), the same ones the device voxelizer
+// uses.  Every arithmetic operation is one IEEE float operation; build with
+// -ffp-contract=off.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+#include "../f1-wind-tunnel_gb300/csrc/wt_fmath.h"
+
+namespace rt {
+
+typedef float f32;
+typedef int32_t i32;
+typedef uint32_t u32;
+template <class T> using atomic = T;
+
+// ---- scalar conversions -------------------------------------------------
+static inline f32 to_f32(f32 x) { return x; }
+static inline f32 to_f32(i32 x) { return (f32)x; }
+static inline f32 to_f32(u32 x) { return (f32)x; }
+static inline f32 to_f32(bool x) { return x ? 1.0f : 0.0f; }
+static inline i32 to_i32(i32 x) { return x; }
+static inline i32 to_i32(u32 x) { return (i32)x; }
+static inline i32 to_i32(bool x) { return x ? 1 : 0; }
+static inline i32 to_i32(f32 x) {
+  if (!(x == x)) return 0;
+  if (x >= 2147483520.0f) return 2147483647;
+  if (x <= -2147483648.0f) return (i32)0x80000000u;
+  return (i32)x;
+}
+static inline u32 to_u32(u32 x) { return x; }
+static inline u32 to_u32(i32 x) { return (u32)x; }
+static inline u32 to_u32(bool x) { return x ? 1u : 0u; }
+static inline u32 to_u32(f32 x) {
+  if (!(x == x)) return 0u;
+  if (x <= 0.0f) return 0u;
+  if (x >= 4294967040.0f) return 4294967295u;
+  return (u32)x;
+}
+template <class T> struct conv;
+template <> struct conv<f32> { template <class S> static f32 c(S s) { return to_f32(s); } };
+template <> struct conv<i32> { template <class S> static i32 c(S s) { return to_i32(s); } };
+template <> struct conv<u32> { template <class S> static u32 c(S s) { return to_u32(s); } };
+// abstract-int literals (C++ int) and other arithmetic types
+template <class T, class S> static inline T cv(S s) { return conv<T>::c(s); }
+template <> inline f32 cv<f32, double>(double s) { return (f32)s; }
+
+// ---- vectors ------------------------------------------------------------
+template <class T> struct vec2;
+template <class T> struct vec3;
+template <class T> struct vec4;
+
+template <class T> struct vec2 {
+  T x, y;
+  vec2() : x(0), y(0) {}
+  template <class S> explicit vec2(S s) : x(cv<T>(s)), y(cv<T>(s)) {}
+  template <class A, class B> vec2(A a, B b) : x(cv<T>(a)), y(cv<T>(b)) {}
+  template <class S> vec2(const vec2<S>& v) : x(cv<T>(v.x)), y(cv<T>(v.y)) {}
+  vec2(const vec2& v) = default;
+  vec2& operator=(const vec2& v) = default;
+};
+template <class T> struct vec3 {
+  T x, y, z;
+  vec3() : x(0), y(0), z(0) {}
+  template <class S> explicit vec3(S s) : x(cv<T>(s)), y(cv<T>(s)), z(cv<T>(s)) {}
+  template <class A, class B, class C> vec3(A a, B b, C c) : x(cv<T>(a)), y(cv<T>(b)), z(cv<T>(c)) {}
+  template <class S, class C> vec3(const vec2<S>& ab, C c) : x(cv<T>(ab.x)), y(cv<T>(ab.y)), z(cv<T>(c)) {}
+  template <class S> vec3(const vec3<S>& v) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(v.z)) {}
+  vec3(const vec3& v) = default;
+  vec3& operator=(const vec3& v) = default;
+  vec2<T> xy() const { return vec2<T>(x, y); }
+  vec2<T> yz() const { return vec2<T>(y, z); }
+};
+template <class T> struct vec4 {
+  T x, y, z, w;
+  vec4() : x(0), y(0), z(0), w(0) {}
+  template <class S> explicit vec4(S s) : x(cv<T>(s)), y(cv<T>(s)), z(cv<T>(s)), w(cv<T>(s)) {}
+  template <class A, class B, class C, class D>
+  vec4(A a, B b, C c, D d) : x(cv<T>(a)), y(cv<T>(b)), z(cv<T>(c)), w(cv<T>(d)) {}
+  template <class S, class D> vec4(const vec3<S>& v, D d) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(v.z)), w(cv<T>(d)) {}
+  template <class S> vec4(const vec4<S>& v) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(v.z)), w(cv<T>(v.w)) {}
+  vec4(const vec4& v) = default;
+  vec4& operator=(const vec4& v) = default;
+  vec2<T> xy() const { return vec2<T>(x, y); }
+  vec2<T> zw() const { return vec2<T>(z, w); }
+  vec3<T> xyz() const { return vec3<T>(x, y, z); }
+};
+typedef vec2<f32> vec2f; typedef vec3<f32> vec3f; typedef vec4<f32> vec4f;
+typedef vec2<i32> vec2i; typedef vec3<i32> vec3i; typedef vec4<i32> vec4i;
+typedef vec2<u32> vec2u; typedef vec3<u32> vec3u; typedef vec4<u32> vec4u;
+
+#define RT_VOP(OP)                                                                                  \
+  template <class T> vec2<T> operator OP(const vec2<T>& a, const vec2<T>& b) { return vec2<T>(a.x OP b.x, a.y OP b.y); } \
+  template <class T> vec3<T> operator OP(const vec3<T>& a, const vec3<T>& b) { return vec3<T>(a.x OP b.x, a.y OP b.y, a.z OP b.z); } \
+  template <class T> vec4<T> operator OP(const vec4<T>& a, const vec4<T>& b) { return vec4<T>(a.x OP b.x, a.y OP b.y, a.z OP b.z, a.w OP b.w); } \
+  template <class T, class S> vec2<T> operator OP(const vec2<T>& a, S s) { T b = cv<T>(s); return vec2<T>(a.x OP b, a.y OP b); } \
+  template <class T, class S> vec3<T> operator OP(const vec3<T>& a, S s) { T b = cv<T>(s); return vec3<T>(a.x OP b, a.y OP b, a.z OP b); } \
+  template <class T, class S> vec4<T> operator OP(const vec4<T>& a, S s) { T b = cv<T>(s); return vec4<T>(a.x OP b, a.y OP b, a.z OP b, a.w OP b); } \
+  template <class T, class S> vec2<T> operator OP(S s, const vec2<T>& b) { T a = cv<T>(s); return vec2<T>(a OP b.x, a OP b.y); } \
+  template <class T, class S> vec3<T> operator OP(S s, const vec3<T>& b) { T a = cv<T>(s); return vec3<T>(a OP b.x, a OP b.y, a OP b.z); } \
+  template <class T, class S> vec4<T> operator OP(S s, const vec4<T>& b) { T a = cv<T>(s); return vec4<T>(a OP b.x, a OP b.y, a OP b.z, a OP b.w); } \
+  template <class T, class S> vec2<T>& operator OP##=(vec2<T>& a, const S& b) { a = a OP b; return a; } \
+  template <class T, class S> vec3<T>& operator OP##=(vec3<T>& a, const S& b) { a = a OP b; return a; } \
+  template <class T, class S> vec4<T>& operator OP##=(vec4<T>& a, const S& b) { a = a OP b; return a; }
+RT_VOP(+)
+RT_VOP(-)
+RT_VOP(*)
+RT_VOP(/)
+#undef RT_VOP
+template <class T> vec2<T> operator-(const vec2<T>& a) { return vec2<T>(-a.x, -a.y); }
+template <class T> vec3<T> operator-(const vec3<T>& a) { return vec3<T>(-a.x, -a.y, -a.z); }
+template <class T> vec4<T> operator-(const vec4<T>& a) { return vec4<T>(-a.x, -a.y, -a.z, -a.w); }
+
+// ---- fixed-size arrays ---------------------------------------------------
+template <class T, int N> struct array {
+  T a[N];
+  array() { for (int i = 0; i < N; i++) a[i] = T(); }
+  template <class... A> explicit array(A... xs) : a{cv_elem(xs)...} {}
+  template <class S> static T cv_elem(const S& s) { return T(s); }
+  static T cv_elem(int s) { return cv<T>(s); }
+  static T cv_elem(double s) { return (T)s; }
+  T& operator[](int64_t i) { return a[i]; }
+  const T& operator[](int64_t i) const { return a[i]; }
+};
+
+// ---- storage buffers: a shared pointer binding ----------------------------
+template <class T> struct storage {
+  T* p = nullptr;
+  T& operator[](int64_t i) const { return p[i]; }
+};
+struct texture3d { int dummy = 0; };
+struct sampler { int dummy = 0; };
+// Textures only feed the baked-mesh (W17) scene, which this model does not evaluate.
+static inline vec4f textureSampleLevel(const texture3d&, const sampler&, vec3f, f32) { return vec4f(0.0f); }
+static inline vec3u textureDimensions(const texture3d&) { return vec3u(1u, 1u, 1u); }
+
+// ---- builtins -----------------------------------------------------------
+static inline f32 abs(f32 x) { return x < 0.0f ? -x : (x == 0.0f ? 0.0f : x); }
+static inline i32 abs(i32 x) { return x < 0 ? (i32)(0u - (u32)x) : x; }
+template <class T> vec2<T> abs(const vec2<T>& v) { return vec2<T>(abs(v.x), abs(v.y)); }
+template <class T> vec3<T> abs(const vec3<T>& v) { return vec3<T>(abs(v.x), abs(v.y), abs(v.z)); }
+
+static inline f32 min(f32 a, f32 b) { return b < a ? b : a; }
+static inline f32 max(f32 a, f32 b) { return a < b ? b : a; }
+static inline i32 min(i32 a, i32 b) { return b < a ? b : a; }
+static inline i32 max(i32 a, i32 b) { return a < b ? b : a; }
+static inline u32 min(u32 a, u32 b) { return b < a ? b : a; }
+static inline u32 max(u32 a, u32 b) { return a < b ? b : a; }
+template <class T> vec2<T> min(const vec2<T>& a, const vec2<T>& b) { return vec2<T>(min(a.x, b.x), min(a.y, b.y)); }
+template <class T> vec3<T> min(const vec3<T>& a, const vec3<T>& b) { return vec3<T>(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)); }
+template <class T> vec2<T> max(const vec2<T>& a, const vec2<T>& b) { return vec2<T>(max(a.x, b.x), max(a.y, b.y)); }
+template <class T> vec3<T> max(const vec3<T>& a, const vec3<T>& b) { return vec3<T>(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }
+template <class T> T clamp(const T& e, const T& lo, const T& hi) { return min(max(e, lo), hi); }
+
+static inline f32 mix(f32 a, f32 b, f32 t) { return a * (1.0f - t) + b * t; }
+template <class T> vec2<T> mix(const vec2<T>& a, const vec2<T>& b, f32 t) { return vec2<T>(mix(a.x, b.x, t), mix(a.y, b.y, t)); }
+template <class T> vec3<T> mix(const vec3<T>& a, const vec3<T>& b, f32 t) { return vec3<T>(mix(a.x, b.x, t), mix(a.y, b.y, t), mix(a.z, b.z, t)); }
+static inline f32 smoothstep(f32 lo, f32 hi, f32 x) {
+  f32 t = clamp((x - lo) / (hi - lo), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+template <class T> static inline T select(const T& f, const T& t, bool c) { return c ? t : f; }
+
+static inline f32 sqrt(f32 x) { return __builtin_sqrtf(x); }
+static inline f32 floor(f32 x) { return __builtin_floorf(x); }
+template <class T> vec2<T> floor(const vec2<T>& v) { return vec2<T>(floor(v.x), floor(v.y)); }
+template <class T> vec3<T> floor(const vec3<T>& v) { return vec3<T>(floor(v.x), floor(v.y), floor(v.z)); }
+static inline f32 round(f32 x) { return __builtin_rintf(x); }
+static inline f32 sign(f32 x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+static inline f32 sin(f32 x) { return wtm::sinf(x); }
+static inline f32 cos(f32 x) { return wtm::cosf(x); }
+static inline f32 atan(f32 x) { return wtm::atanf(x); }
+
+static inline f32 dot(const vec2f& a, const vec2f& b) { return a.x * b.x + a.y * b.y; }
+static inline f32 dot(const vec3f& a, const vec3f& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline f32 dot(const vec4f& a, const vec4f& b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+static inline f32 length(f32 x) { return abs(x); }
+template <class V> static inline f32 length(const V& v) { return sqrt(dot(v, v)); }
+
+template <class T> static inline T bitcast(f32 x) { T r; memcpy(&r, &x, 4); return r; }
+
+// Atomics: relaxed read-modify-write on plain memory, two's-complement wrap.
+template <class T> static inline T atomicAdd(T* p, T v) { return __atomic_fetch_add(p, v, __ATOMIC_RELAXED); }
+template <class T> static inline void atomicStore(T* p, T v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
+template <class T> static inline T atomicLoad(T* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
+
+}  // namespace rt
+
+#define RT_USING                                                                                 \
+  using rt::f32; using rt::i32; using rt::u32; using rt::atomic; using rt::array; using rt::storage; \
+  using rt::vec2f; using rt::vec3f; using rt::vec4f; using rt::vec2i; using rt::vec3i; using rt::vec4i; \
+  using rt::vec2u; using rt::vec3u; using rt::vec4u; using rt::texture3d; using rt::sampler;         \
+  using rt::to_f32; using rt::to_i32; using rt::to_u32; using rt::abs; using rt::min; using rt::max; \
+  using rt::clamp; using rt::mix; using rt::smoothstep; using rt::select; using rt::sqrt;            \
+  using rt::floor; using rt::round; using rt::sign; using rt::sin; using rt::cos; using rt::atan;    \
+  using rt::dot; using rt::length; using rt::bitcast; using rt::atomicAdd; using rt::atomicStore;   \
+  using rt::atomicLoad; using rt::textureSampleLevel; using rt::textureDimensions;
