@@ -1,0 +1,328 @@
+#!/usr/bin/env python3
+"""Benchmark of the wind-tunnel simulation step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl wt|reference]
+                    [--workload f1|cube] [--storage f32|f16|bf16]
+
+One bench step = one frame of the reference engine's compute pass
+(src/engine/engine.ts:708-712) at the headless check's 8 steps per frame:
+8 D3Q19 collide-stream steps + 2 semi-Lagrangian heat passes, with the
+per-component forces recorded every step.  Default workload: the generic
+analytic F1 voxelized at 4.5 cm into a 256x96x80 half tunnel (FP32, moving
+belt, heat from brakes/exhaust/radiator at T=1), synthetic geometry from a
+seeded shape.  The lattice (157 MB of populations and cell words) is larger
+than the 126 MB L2, so no flush is needed between timed steps.
+
+value   = MLUPS over the timed frames (inputs resident in HBM, CUDA events on
+          the library's stream, max over ranks).
+e2e     = the same metric through the public Python API (ctypes -> C ABI) with
+          a per-frame parameter upload from host memory and a per-frame force
+          readback to host, host wall clock.
+roofline: the collide-stream kernel alone, 156 algorithmic B per lattice update
+          (f32; 80 B for f16/bf16) over its CUDA-event duration.
+cpu_baseline: the reference's shader arithmetic on the host cores (translated
+          reference build when present, else the oracle port), bounded sample.
+Multi-GPU (torchrun, N>1): independent replicas, one lattice per GPU (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "f1-wind-tunnel_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+THROTTLE_BITS = {
+    0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
+    0x10: "sync_boost", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+    0x100: "display_clock_setting",
+}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active"
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 5:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+                bits = int(parts[4], 16) if parts[4].startswith("0x") else int(parts[4])
+            except ValueError:
+                continue
+            for b, name in THROTTLE_BITS.items():
+                if bits & b and name != "gpu_idle":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(storage):
+    """Per-launch DRAM bytes of the collide-stream kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "collide_stream_traffic.json")) as f:
+            t = json.load(f)
+        return t.get(storage)
+    except (OSError, ValueError):
+        return None
+
+
+def workload(args, rank):
+    import windtunnel
+    if args.workload == "cube":
+        dims, origin, h, sim, shape = windtunnel.cube_config(storage=args.storage)
+        desc = "half tunnel 128x64x64, cube edge 22 cells at x=40 on the floor, u_in 0.08, tau0 0.51, Cs 0.1, sponge 16"
+    else:
+        dims, origin, h, sim, shape = windtunnel.f1_config(seed=args.seed + rank, storage=args.storage)
+        desc = ("generic analytic F1 voxelized at 4.5 cm into a 256x96x80 half tunnel, seeded wing angles 5-25 deg, "
+                "moving belt, heat sources at T=1, u_in 0.08, tau0 0.51, Cs 0.1, sponge 16")
+    return dims, origin, h, sim, shape, desc
+
+
+def cpu_baseline(args, seconds_budget=20.0):
+    """The reference's arithmetic on all host cores, bounded sample of the same workload."""
+    import windtunnel
+    from oracle import pyoracle
+    dims, origin, h, sim, shape, _ = workload(args, 0)
+    kind = "reference" if pyoracle.ref_lib() is not None and args.storage == "f32" else "port"
+    if kind == "reference":
+        m = pyoracle.Reference(dims, origin, h, sim)
+        threads = pyoracle.ref_lib().wtr_threads()
+    else:
+        m = pyoracle.Oracle(dims, origin, h, sim)
+        threads = pyoracle.oracle_lib().wto_threads()
+    m.voxelize(shape)
+    m.reset()
+    n = int(dims[0] * dims[1] * dims[2])
+    m.frame(2)  # warm-up
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        m.frame(8)
+        frames += 1
+        el = time.perf_counter() - t0
+        if el > seconds_budget or frames >= args.cpu_frames:
+            break
+    mlups = n * 8 * frames / el / 1e6
+    sample = f"{frames} frames x (8 LBM steps + 2 heat passes) of the {dims[0]}x{dims[1]}x{dims[2]} workload"
+    return {"value": mlups, "unit": "MLUPS", "cores": int(threads), "kind": kind, "sample": sample,
+            "seconds": el}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    base = cpu_baseline(args, seconds_budget=args.ref_seconds)
+    dims = workload(args, 0)[:1][0]
+    line = {
+        "metric": "MLUPS", "value": base["value"], "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload(args, 0)[5], "cells": int(dims[0] * dims[1] * dims[2]),
+                   "lbm_steps_per_step": 8, "heat_passes_per_step": 2},
+        "cpu_baseline": {"value": base["value"], "unit": "MLUPS", "cores": base["cores"], "kind": base["kind"],
+                         "sample": base["sample"]},
+        "e2e": {"value": base["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200, help="timed frames")
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="wt", choices=["wt", "reference"])
+    ap.add_argument("--workload", default="f1", choices=["f1", "cube"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-frames", type=int, default=4)
+    ap.add_argument("--ref-seconds", type=float, default=60.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-steps", type=int, default=64, help="LBM steps per kernel-timing launch batch")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        import __graft_entry__ as ge
+        ge._build_oracle()
+        run_reference_arm(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+    if rank == 0:
+        ge.build()
+    if dist:
+        dist.barrier()
+    torch.cuda.set_device(local)
+    torch.cuda.init()
+    import windtunnel
+    from windtunnel.workloads import bytes_per_lup
+
+    dims, origin, h, sim, shape, desc = workload(args, rank)
+    n = int(dims[0] * dims[1] * dims[2])
+    eng = windtunnel.AeroEngine(dims=dims, origin=origin, h=h, sim=sim)
+    eng.set_shape_raw(shape)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+    lbm_per_frame = 8
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- warm-up
+    for _ in range(max(3, args.warmup)):
+        eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0)
+    eng.read_forces_raw()
+    barrier()
+
+    # ---- timed device region: K frames, inputs resident in HBM
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms)
+    frames = args.steps
+    total_cells = n * world
+    value = total_cells * lbm_per_frame * frames / (ms / 1e3) / 1e6
+    fr = eng.read_forces_raw()
+    if fr.guarded:
+        print(f"warning: {fr.guarded} cells hit the divergence guard", file=sys.stderr)
+    launches_per_frame = lbm_per_frame + (lbm_per_frame + 63) // 64 + 2
+
+    # ---- the collide-stream kernel alone: batches of kernel_steps steps, no heat
+    ks = max(2, args.kernel_steps - args.kernel_steps % 2)
+    reps = max(2, 512 // ks)
+    eng.step(ks, 0)
+    barrier()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for _ in range(reps):
+        eng.step(ks, 0)
+    k1.record(stream)
+    barrier()
+    kms = k0.elapsed_time(k1) / (reps * ks)  # per LBM step (one reduction launch per ks steps included)
+    bpl = bytes_per_lup(args.storage)
+    achieved = n * bpl / (kms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # ---- end to end through the public API: per-frame parameter upload + force readback
+    e2e_frames = max(5, min(args.steps, 100))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_frames):
+        eng.set_sim(sim)                     # Sim uniform + sponge table upload (syncSim, engine.ts:497)
+        eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0)
+        eng.read_forces_raw(reset=True)      # maybeReadForces readback (engine.ts:746-747)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = total_cells * lbm_per_frame * e2e_frames / e2e_s / 1e6
+    h2d = dims[0] * 4
+    d2h = 18 * 8 + 12 * 4 + 4
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(args)
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": frames,
+            "warmup": max(3, args.warmup), "ms_per_step": ms / frames, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.storage, "data": "synthetic",
+            "config": {
+                "workload": desc, "cells": n, "lattice": list(dims), "lbm_steps_per_step": lbm_per_frame,
+                "heat_passes_per_step": 2, "storage": args.storage, "parallelism": f"replicas x{world}",
+                "l2": "working set (populations + cell words) larger than the 126 MB L2; no flush",
+            },
+            "roofline": {
+                "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profiled_traffic(args.storage), "peak_source": peak_kind,
+                "kernel": "collide-stream step", "algorithmic_bytes_per_lup": bpl,
+                "kernel_ms_per_step": kms, "kernel_mlups": n / (kms / 1e3) / 1e6,
+            },
+            "cpu_baseline": base,
+            "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_frame * frames,
+            "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

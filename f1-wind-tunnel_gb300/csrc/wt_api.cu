@@ -1,0 +1,486 @@
+// The C ABI of libwt (include/wt.h): context lifetime, device memory, the
+// engine calls of the reference (src/engine/engine.ts AeroEngine: constructor
+// :226, reset :371, setShape :426, frame :574-729, maybeReadForces :739,
+// debugRead :763) mapped onto the device kernels, and error reporting.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "wt_fmath.h"
+#include "wt_internal.h"
+#include "wt_lattice.cuh"
+
+using namespace wt;
+
+struct wt_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  wt_grid grid{};
+  wt_sim sim{};
+  uint32_t nx = 0, ny = 0, nz = 0;
+  uint64_t n = 0, np = 0;
+  size_t elem = 4;
+  StepGeom geom{};
+  uint32_t sm_count = 0;
+  // device buffers
+  void* pop = nullptr;
+  uint32_t* cellw = nullptr;
+  uint8_t* solid = nullptr;
+  float* emit = nullptr;
+  float4* fields = nullptr;
+  float* tA = nullptr;
+  float* tB = nullptr;
+  float4* outlet_u = nullptr;
+  float* tau0_x = nullptr;
+  int32_t* block_slot = nullptr;
+  ForceSlot* slots = nullptr;
+  uint32_t slot_cap = 0;      // records allocated
+  uint32_t nslots = 0;        // records per step for the current scene
+  uint32_t pending_cap = 1;   // steps per reduction launch
+  double* mass_partial = nullptr;
+  double* hist = nullptr;
+  double* totals = nullptr;   // [9] FP64 force sums, [9] mass
+  int32_t* raw_totals = nullptr;  // [12]
+  unsigned int* counters = nullptr;  // [0] guard count, [1] reduce counter
+  // host state
+  uint64_t steps_total = 0, steps_since_read = 0, steps_recorded = 0;
+  uint64_t device_bytes = 0;
+  uint32_t fluid_cells = 0, solid_cells[3] = {0, 0, 0};
+  float ks2 = 0.0f;
+  float feq_in[19];
+  float floor_k[19];
+  std::vector<float> tau_host;  // staging copy of tau0_x (pageable: copied before the call returns)
+  std::string err;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(wt_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+#define WT_CUDA(c, call)                                                                       \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail((c), e_ == cudaErrorMemoryAllocation ? WT_ERR_NOMEM : WT_ERR_CUDA,           \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                         \
+  } while (0)
+
+// WGSL smoothstep/min/max (host copy of the same float arithmetic).
+float h_min(float a, float b) { return b < a ? b : a; }
+float h_max(float a, float b) { return a < b ? b : a; }
+float h_smooth(float lo, float hi, float x) {
+  const float t = h_min(h_max((x - lo) / (hi - lo), 0.0f), 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+
+bool valid_storage(uint32_t s) { return s == WT_STORE_F32 || s == WT_STORE_F16 || s == WT_STORE_BF16; }
+
+template <class T>
+int dalloc(wt_ctx* c, T** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) return fail(c, WT_ERR_NOMEM, std::string("cudaMalloc ") + std::to_string(bytes) + " B: " + cudaGetErrorString(e));
+  c->device_bytes += bytes;
+  return WT_OK;
+}
+
+// Per-parameter tables: x-dependent tau0 (wgsl.ts:260), Smagorinsky factor,
+// inlet equilibrium, belt coefficients.
+int apply_sim(wt_ctx* c) {
+  const wt_sim& s = c->sim;
+  std::vector<float>& t0 = c->tau_host;
+  t0.resize(c->nx);
+  const float fnx = (float)c->nx;
+  for (uint32_t x = 0; x < c->nx; x++) {
+    const float fx = (float)x;
+    t0[x] = s.tau0 + s.sponge_amp * h_smooth(fnx - s.sponge_cells, fnx - 1.0f, fx) +
+            s.inlet_amp * (1.0f - h_smooth(0.0f, s.inlet_cells, fx));
+  }
+  WT_CUDA(c, cudaMemcpyAsync(c->tau0_x, t0.data(), c->nx * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  const float K = 0x1.974b24p+4f;  // 18 * 1.41421356 evaluated as an abstract constant, rounded once
+  c->ks2 = K * s.smag * s.smag;
+  for (int i = 0; i < 19; i++) {
+    const float u = s.u_in;
+    const float cu = (float)CXd(i) * u + (float)CYd(i) * 0.0f + (float)CZd(i) * 0.0f;
+    const float uu = u * u + 0.0f * 0.0f + 0.0f * 0.0f;
+    c->feq_in[i] = Wd(i) * 1.0f * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
+    c->floor_k[i] = 6.0f * Wd(i) * (float)CXd(i);
+  }
+  return WT_OK;
+}
+
+// After new flags: cell words, force-carrying blocks and their partial slots.
+int rebuild_links(wt_ctx* c) {
+  WT_CUDA(c, launch_cell_words(c->solid, c->emit, c->cellw, c->nx, c->ny, c->nz, c->stream));
+  uint8_t* dflags = nullptr;
+  WT_CUDA(c, cudaMallocAsync((void**)&dflags, c->geom.nblocks, c->stream));
+  WT_CUDA(c, launch_block_flags(c->cellw, c->geom, c->nx, c->ny, c->nz, dflags, c->stream));
+  std::vector<uint8_t> flags(c->geom.nblocks);
+  std::vector<uint8_t> sol(c->n);
+  WT_CUDA(c, cudaMemcpyAsync(flags.data(), dflags, c->geom.nblocks, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(sol.data(), c->solid, c->n, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaFreeAsync(dflags, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  std::vector<int32_t> map(c->geom.nblocks);
+  uint32_t ns = 0;
+  for (uint32_t b = 0; b < c->geom.nblocks; b++) map[b] = flags[b] ? (int32_t)ns++ : -1;
+  c->nslots = ns;
+  c->fluid_cells = 0;
+  c->solid_cells[0] = c->solid_cells[1] = c->solid_cells[2] = 0;
+  for (uint64_t i = 0; i < c->n; i++) {
+    if (sol[i] == 0) c->fluid_cells++;
+    else c->solid_cells[(sol[i] - 1) % 3]++;
+  }
+  // Partial records for up to WT_PENDING_MAX steps, capped at 64 MiB.
+  uint64_t per_step = (uint64_t)(ns ? ns : 1) * sizeof(ForceSlot);
+  uint64_t cap_steps = (64ull << 20) / per_step;
+  if (cap_steps < 2) cap_steps = 2;
+  if (cap_steps > WT_PENDING_MAX) cap_steps = WT_PENDING_MAX;
+  const uint64_t need = cap_steps * (ns ? ns : 1);
+  if (need > c->slot_cap) {
+    if (c->slots) {
+      cudaFree(c->slots);
+      c->device_bytes -= (uint64_t)c->slot_cap * sizeof(ForceSlot);
+      c->slots = nullptr;
+    }
+    int rc = dalloc(c, &c->slots, need * sizeof(ForceSlot));
+    if (rc) return rc;
+    c->slot_cap = (uint32_t)need;
+  }
+  c->pending_cap = (uint32_t)cap_steps;
+  WT_CUDA(c, cudaMemcpyAsync(c->block_slot, map.data(), map.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int check_ctx(wt_ctx* c) {
+  if (!c) return WT_ERR_ARG;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(c, WT_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  return WT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* wt_version(void) { return "libwt 0.1 sm_103a"; }
+
+const char* wt_last_error(const wt_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int wt_create(const wt_grid* grid, const wt_sim* sim, wt_ctx** out) {
+  if (!grid || !sim || !out) return fail(nullptr, WT_ERR_ARG, "wt_create: null argument");
+  *out = nullptr;
+  if (grid->nx < 8 || grid->ny < 2 || grid->nz < 2) return fail(nullptr, WT_ERR_ARG, "wt_create: grid must be at least 8x2x2");
+  const uint64_t n = (uint64_t)grid->nx * grid->ny * grid->nz;
+  const uint64_t np = (n + 63) / 64 * 64;
+  if (np * 19 >= (1ull << 32)) return fail(nullptr, WT_ERR_ARG, "wt_create: lattice too large (19 * cells must stay below 2^32)");
+  if (!(grid->h > 0.0f)) return fail(nullptr, WT_ERR_ARG, "wt_create: cell size must be positive");
+  if (!valid_storage(sim->storage)) return fail(nullptr, WT_ERR_ARG, "wt_create: unknown storage format");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(nullptr, WT_ERR_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, dev);
+  if (e != cudaSuccess) return fail(nullptr, WT_ERR_DEVICE, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
+  if (!(prop.major == 10 && prop.minor == 3))
+    return fail(nullptr, WT_ERR_DEVICE, "libwt is built for sm_103a (GB300); device " + std::string(prop.name) + " is sm_" +
+                                            std::to_string(prop.major) + std::to_string(prop.minor));
+  wt_ctx* c = new wt_ctx();
+  c->device = dev;
+  c->grid = *grid;
+  c->sim = *sim;
+  c->nx = grid->nx; c->ny = grid->ny; c->nz = grid->nz;
+  c->n = n; c->np = np;
+  c->elem = sim->storage == WT_STORE_F32 ? 4 : 2;
+  c->sm_count = prop.multiProcessorCount;
+  uint32_t bx = 128;
+  if (const char* s = getenv("WT_STEP_BX")) bx = (uint32_t)atoi(s);
+  c->geom = step_geometry(c->nx, c->ny, c->nz, bx);
+  int rc = 0;
+  auto cleanup = [&](int code) { std::string m = c->err; wt_destroy(c); g_create_error = m; return code; };
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { c->err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return cleanup(WT_ERR_CUDA); }
+  if ((rc = dalloc(c, &c->pop, 19 * np * c->elem)) || (rc = dalloc(c, &c->cellw, n * 4)) ||
+      (rc = dalloc(c, &c->solid, n)) || (rc = dalloc(c, &c->emit, n * 4)) || (rc = dalloc(c, &c->fields, n * 16)) ||
+      (rc = dalloc(c, &c->tA, n * 4)) || (rc = dalloc(c, &c->tB, n * 4)) ||
+      (rc = dalloc(c, &c->outlet_u, (uint64_t)c->ny * c->nz * 16)) || (rc = dalloc(c, &c->tau0_x, c->nx * 4)) ||
+      (rc = dalloc(c, &c->block_slot, (uint64_t)c->geom.nblocks * 4)) ||
+      (rc = dalloc(c, &c->mass_partial, (uint64_t)c->geom.nblocks * 8)) ||
+      (rc = dalloc(c, &c->hist, (uint64_t)WT_HIST_CAP * 16 * 8)) || (rc = dalloc(c, &c->totals, 18 * 8)) ||
+      (rc = dalloc(c, &c->raw_totals, 12 * 4)) || (rc = dalloc(c, &c->counters, 4 * 4)))
+    return cleanup(rc);
+  if (cudaMemsetAsync(c->solid, 0, n, c->stream) != cudaSuccess || cudaMemsetAsync(c->emit, 0, n * 4, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->totals, 0, 18 * 8, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->raw_totals, 0, 48, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->counters, 0, 16, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->pop, 0, 19 * np * c->elem, c->stream) != cudaSuccess) {
+    c->err = "initial cudaMemsetAsync failed";
+    return cleanup(WT_ERR_CUDA);
+  }
+  if ((rc = apply_sim(c)) || (rc = rebuild_links(c)) || (rc = wt_reset(c))) return cleanup(rc);
+  *out = c;
+  return WT_OK;
+}
+
+int wt_destroy(wt_ctx* c) {
+  if (!c) return WT_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
+                  c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return WT_OK;
+}
+
+int wt_set_sim(wt_ctx* c, const wt_sim* sim) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!sim) return fail(c, WT_ERR_ARG, "wt_set_sim: null sim");
+  if (sim->storage != c->sim.storage) return fail(c, WT_ERR_ARG, "wt_set_sim: storage format is fixed at wt_create");
+  c->sim = *sim;
+  return apply_sim(c);
+}
+
+int wt_reset(wt_ctx* c) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  WT_CUDA(c, launch_init(c->sim.storage, c->pop, c->fields, c->outlet_u, c->nx, c->ny, c->nz, c->np, c->sim.u_in, c->stream));
+  WT_CUDA(c, cudaMemsetAsync(c->tA, 0, c->n * 4, c->stream));
+  WT_CUDA(c, cudaMemsetAsync(c->tB, 0, c->n * 4, c->stream));
+  c->steps_total = 0;
+  return WT_OK;
+}
+
+int wt_voxelize(wt_ctx* c, const wt_shape* shape) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!shape) return fail(c, WT_ERR_ARG, "wt_voxelize: null shape");
+  const uint32_t k = shape->kind;
+  if (!(k == WT_KIND_F1 || k == WT_KIND_SPHERE || k == WT_KIND_CUBE || k == WT_KIND_WING || k == WT_KIND_EMPTY ||
+        k == WT_KIND_BOX))
+    return fail(c, WT_ERR_UNSUPPORTED, "wt_voxelize: scene kind " + std::to_string(k) +
+                                           " is not built (custom profile and baked-mesh scenes)");
+  WT_CUDA(c, launch_voxelize(*shape, c->grid, c->solid, c->emit, c->stream));
+  return rebuild_links(c);
+}
+
+int wt_set_solid(wt_ctx* c, const uint32_t* solid, const float* emit) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!solid || !emit) return fail(c, WT_ERR_ARG, "wt_set_solid: null buffer");
+  uint32_t* tmp = nullptr;
+  WT_CUDA(c, cudaMallocAsync((void**)&tmp, c->n * 4, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(tmp, solid, c->n * 4, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, launch_solid_from_u32(tmp, c->solid, c->n, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(c->emit, emit, c->n * 4, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaFreeAsync(tmp, c->stream));
+  return rebuild_links(c);
+}
+
+int wt_step(wt_ctx* c, int n_lbm_steps, int heat_passes, float heat_dt) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (n_lbm_steps < 2 || (n_lbm_steps & 1))
+    return fail(c, WT_ERR_ARG, "wt_step: n_lbm_steps must be even and >= 2 (the engine issues max(2, steps - steps % 2))");
+  if (heat_passes < 0 || (heat_passes & 1)) return fail(c, WT_ERR_ARG, "wt_step: heat_passes must be 0 or even");
+  StepArgs a;
+  a.pop = c->pop; a.cellw = c->cellw; a.solid = c->solid; a.fields = c->fields; a.outlet_u = c->outlet_u;
+  a.tau0_x = c->tau0_x; a.block_slot = c->block_slot; a.mass_partial = c->mass_partial;
+  a.guard_count = c->counters;
+  a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.n = c->n; a.np = c->np;
+  a.u_in = c->sim.u_in; a.ks2 = c->ks2;
+  memcpy(a.feq_in, c->feq_in, sizeof(a.feq_in));
+  memcpy(a.floor_k, c->floor_k, sizeof(a.floor_k));
+  uint32_t pending = 0;
+  for (int s = 0; s < n_lbm_steps; s++) {
+    const bool last = (s == n_lbm_steps - 1);
+    a.slots = c->slots + (size_t)pending * (c->nslots ? c->nslots : 1);
+    WT_CUDA(c, launch_step(c->sim.storage, (s & 1) == 0, last, c->geom, a, c->stream));
+    pending++;
+    if (pending == c->pending_cap || last) {
+      WT_CUDA(c, launch_force_reduce(c->slots, c->nslots, pending, c->hist, WT_HIST_CAP, c->steps_recorded, c->totals,
+                                     c->raw_totals, c->mass_partial, last ? c->geom.nblocks : 0, c->totals + 9,
+                                     c->counters + 1, c->stream));
+      c->steps_recorded += pending;
+      pending = 0;
+    }
+  }
+  c->steps_total += n_lbm_steps;
+  c->steps_since_read += n_lbm_steps;
+  if (heat_passes > 0) {
+    HeatArgs h;
+    h.fields = c->fields; h.emit = c->emit;
+    h.nx = c->nx; h.ny = c->ny; h.nz = c->nz;
+    h.dt = heat_dt > 0.0f ? heat_dt : (float)n_lbm_steps / 2.0f;
+    h.cool = c->sim.heat_cool; h.diffuse = c->sim.heat_diffuse; h.src_mix = c->sim.heat_src_mix;
+    for (int p = 0; p < heat_passes; p++) {
+      h.tin = (p & 1) ? c->tB : c->tA;
+      h.tout = (p & 1) ? c->tA : c->tB;
+      WT_CUDA(c, launch_heat(h, c->stream));
+    }
+  }
+  return WT_OK;
+}
+
+int wt_read_forces(wt_ctx* c, wt_forces* out, int reset) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!out) return fail(c, WT_ERR_ARG, "wt_read_forces: null output");
+  double tot[18];
+  unsigned int g = 0;
+  WT_CUDA(c, cudaMemcpyAsync(tot, c->totals, sizeof(tot), cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(out->raw, c->raw_totals, 48, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(&g, c->counters, 4, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  memcpy(out->sum, tot, sizeof(out->sum));
+  out->mass = tot[9];
+  out->steps = c->steps_since_read;
+  out->guarded = g;
+  if (reset) {
+    WT_CUDA(c, cudaMemsetAsync(c->totals, 0, 9 * 8, c->stream));
+    WT_CUDA(c, cudaMemsetAsync(c->raw_totals, 0, 48, c->stream));
+    WT_CUDA(c, cudaMemsetAsync(c->counters, 0, 4, c->stream));
+    c->steps_since_read = 0;
+  }
+  return WT_OK;
+}
+
+int wt_read_force_history(wt_ctx* c, double* out, uint32_t count) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!out && count) return fail(c, WT_ERR_ARG, "wt_read_force_history: null output");
+  const uint64_t avail = c->steps_recorded < WT_HIST_CAP ? c->steps_recorded : WT_HIST_CAP;
+  if (count > avail) return fail(c, WT_ERR_ARG, "wt_read_force_history: only " + std::to_string(avail) + " steps recorded");
+  std::vector<double> rec((size_t)count * 16);
+  const uint64_t first = c->steps_recorded - count;
+  for (uint32_t k = 0; k < count;) {
+    const uint64_t slot = (first + k) % WT_HIST_CAP;
+    const uint32_t run = (uint32_t)((WT_HIST_CAP - slot) < (count - k) ? (WT_HIST_CAP - slot) : (count - k));
+    WT_CUDA(c, cudaMemcpyAsync(rec.data() + (size_t)k * 16, c->hist + slot * 16, (size_t)run * 16 * 8,
+                               cudaMemcpyDeviceToHost, c->stream));
+    k += run;
+  }
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (uint32_t k = 0; k < count; k++) memcpy(out + (size_t)k * 9, rec.data() + (size_t)k * 16, 9 * 8);
+  return WT_OK;
+}
+
+int wt_read_fields(wt_ctx* c, float* u_rho, uint32_t* solid, float* temps, float* emit, uint32_t* links) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  const uint64_t n = c->n;
+  if (u_rho) WT_CUDA(c, cudaMemcpyAsync(u_rho, c->fields, n * 16, cudaMemcpyDeviceToHost, c->stream));
+  if (temps) WT_CUDA(c, cudaMemcpyAsync(temps, c->tA, n * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (emit) WT_CUDA(c, cudaMemcpyAsync(emit, c->emit, n * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (solid || links) {
+    uint32_t* tmp = nullptr;
+    WT_CUDA(c, cudaMallocAsync((void**)&tmp, n * 4, c->stream));
+    if (solid) {
+      WT_CUDA(c, launch_solid_u32(c->solid, tmp, n, c->stream));
+      WT_CUDA(c, cudaMemcpyAsync(solid, tmp, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (links) {
+      WT_CUDA(c, launch_links_out(c->cellw, tmp, n, c->stream));
+      WT_CUDA(c, cudaMemcpyAsync(links, tmp, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+    WT_CUDA(c, cudaFreeAsync(tmp, c->stream));
+  }
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int wt_read_populations(wt_ctx* c, float* f) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!f) return fail(c, WT_ERR_ARG, "wt_read_populations: null output");
+  float* tmp = nullptr;
+  WT_CUDA(c, cudaMallocAsync((void**)&tmp, c->n * 19 * 4, c->stream));
+  WT_CUDA(c, launch_read_pop(c->sim.storage, c->pop, tmp, (uint32_t)c->n, c->np, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(f, tmp, c->n * 19 * 4, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaFreeAsync(tmp, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int wt_write_state(wt_ctx* c, const float* f, const float* u_rho, const float* temps) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (f) {
+    float* tmp = nullptr;
+    WT_CUDA(c, cudaMallocAsync((void**)&tmp, c->n * 19 * 4, c->stream));
+    WT_CUDA(c, cudaMemcpyAsync(tmp, f, c->n * 19 * 4, cudaMemcpyHostToDevice, c->stream));
+    WT_CUDA(c, launch_write_pop(c->sim.storage, tmp, c->pop, (uint32_t)c->n, c->np, c->stream));
+    WT_CUDA(c, cudaFreeAsync(tmp, c->stream));
+  }
+  if (u_rho) {
+    WT_CUDA(c, cudaMemcpyAsync(c->fields, u_rho, c->n * 16, cudaMemcpyHostToDevice, c->stream));
+    std::vector<float4> ou((size_t)c->ny * c->nz);
+    for (uint32_t z = 0; z < c->nz; z++)
+      for (uint32_t y = 0; y < c->ny; y++) {
+        const uint64_t idx = (uint64_t)(c->nx - 1) + (uint64_t)c->nx * (y + (uint64_t)c->ny * z);
+        ou[y + (size_t)c->ny * z] = make_float4(u_rho[4 * idx], u_rho[4 * idx + 1], u_rho[4 * idx + 2], 0.0f);
+      }
+    WT_CUDA(c, cudaMemcpyAsync(c->outlet_u, ou.data(), ou.size() * 16, cudaMemcpyHostToDevice, c->stream));
+    WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  if (temps) WT_CUDA(c, cudaMemcpyAsync(c->tA, temps, c->n * 4, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int wt_reset_from(wt_ctx* c, const float* u_rho, uint32_t cx, uint32_t cy, uint32_t cz) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!u_rho || cx == 0 || cy == 0 || cz == 0) return fail(c, WT_ERR_ARG, "wt_reset_from: empty coarse field");
+  float4* tmp = nullptr;
+  const size_t bytes = (size_t)cx * cy * cz * 16;
+  WT_CUDA(c, cudaMallocAsync((void**)&tmp, bytes, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(tmp, u_rho, bytes, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, launch_resample_init(c->sim.storage, tmp, cx, cy, cz, c->pop, c->fields, c->outlet_u, c->nx, c->ny, c->nz,
+                                  c->np, c->stream));
+  WT_CUDA(c, cudaFreeAsync(tmp, c->stream));
+  WT_CUDA(c, cudaMemsetAsync(c->tA, 0, c->n * 4, c->stream));
+  WT_CUDA(c, cudaMemsetAsync(c->tB, 0, c->n * 4, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->steps_total = 0;
+  return WT_OK;
+}
+
+int wt_info_get(wt_ctx* c, wt_info* out) {
+  if (!c || !out) return WT_ERR_ARG;
+  out->cells = c->n;
+  out->device_bytes = c->device_bytes;
+  out->steps_total = c->steps_total;
+  out->storage = c->sim.storage;
+  out->fluid_cells = c->fluid_cells;
+  for (int k = 0; k < 3; k++) out->solid_cells[k] = c->solid_cells[k];
+  out->boundary_blocks = c->nslots;
+  out->history_capacity = WT_HIST_CAP;
+  out->sm_count = c->sm_count;
+  return WT_OK;
+}
+
+void* wt_stream(wt_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int wt_sync(wt_ctx* c) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,71 @@
+// Semi-Lagrangian heat advection (HEAT, src/engine/wgsl.ts:460-510): trilinear
+// backtrace of the temperature along u*dt, 6-neighbour diffusion mix, source
+// mix from the voxelizer's emission field, cooling.  One thread per cell; the
+// backtrace gathers stay within a few cells so they hit L1/L2.
+// Algorithmic traffic per cell and pass: fields 16 B + emit 4 B + tin 4 B read,
+// tout 4 B written = 28 B.  Built with -fmad=false: bit-identical to the CPU model.
+#include "wt_internal.h"
+
+namespace wt {
+namespace {
+
+__device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+__device__ __forceinline__ float mxf(float a, float b) { return a < b ? b : a; }
+
+__device__ __forceinline__ uint32_t idx_of(int x, int y, int z, int nx, int ny, int nz) {
+  if (z < 0) z = -z - 1;  // symmetry plane (wgsl.ts:472)
+  x = min(max(x, 0), nx - 1);
+  y = min(max(y, 0), ny - 1);
+  z = min(max(z, 0), nz - 1);
+  return (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+}
+
+__device__ __forceinline__ int f2i(float x) { return __float2int_rz(x); }  // saturating, NaN -> 0
+
+__global__ void heat_kernel(HeatArgs a) {
+  const int nx = (int)a.nx, ny = (int)a.ny, nz = (int)a.nz;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= nx || y >= ny) return;
+  const uint32_t idx = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+  const float4 fv = a.fields[idx];
+  if (fv.w <= 0.0f) {
+    a.tout[idx] = a.emit[idx];
+    return;
+  }
+  const float gx = (float)x - fv.x * a.dt, gy = (float)y - fv.y * a.dt, gz = (float)z - fv.z * a.dt;
+  const int ix = f2i(floorf(gx)), iy = f2i(floorf(gy)), iz = f2i(floorf(gz));
+  const float fx = gx - (float)ix, fy = gy - (float)iy, fz = gz - (float)iz;
+  float t = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int ox = k & 1, oy = (k >> 1) & 1, oz = (k >> 2) & 1;
+    const float w = (ox ? fx : 1.0f - fx) * (oy ? fy : 1.0f - fy) * (oz ? fz : 1.0f - fz);
+    const int cx = ix + ox;
+    const float tv = cx < 0 ? 0.0f : a.tin[idx_of(cx, iy + oy, iz + oz, nx, ny, nz)];
+    t = t + tv * w;
+  }
+  float nb = 0.0f, src = 0.0f;
+  const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const int cx = x + off[k][0], cy = y + off[k][1], cz = z + off[k][2];
+    nb = nb + (cx < 0 ? 0.0f : a.tin[idx_of(cx, cy, cz, nx, ny, nz)]);
+    if (cx >= 0 && cy >= 0 && cx < nx && cy < ny && cz < nz) src = mxf(src, a.emit[idx_of(cx, cy, cz, nx, ny, nz)]);
+  }
+  t = mixf(t, __fdiv_rn(nb, 6.0f), a.diffuse);
+  if (src > 0.0f) t = mixf(t, src, a.src_mix);
+  a.tout[idx] = mxf(t * (1.0f - a.cool), 0.0f);
+}
+
+}  // namespace
+
+cudaError_t launch_heat(const HeatArgs& a, cudaStream_t s) {
+  const dim3 block(128, 1, 1);
+  const dim3 g((a.nx + 127) / 128, a.ny, a.nz);
+  heat_kernel<<<g, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace wt

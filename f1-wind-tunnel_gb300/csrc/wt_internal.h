@@ -1,0 +1,97 @@
+// Internal declarations of libwt: device data layout, kernel argument blocks
+// and launchers shared by the translation units.  Not installed.
+//
+// Device data of one lattice (n = nx*ny*nz cells, np = n rounded up to 64):
+//   pop        19*np populations, one contiguous array per direction, in the
+//              AA in-place layout (see wt_lbm.cu); f32, or f - w_i as f16/bf16
+//   cellw      n  u32 cell words: link bits, solid, belt, duct (wt_lattice.cuh)
+//   solid      n  u8 solid group (0 fluid, 1 body, 2 front wing, 3 rear wing)
+//   emit       n  f32 heat source / duct marker (VOXELIZE output)
+//   fields     n  float4 (ux, uy, uz, rho), written on the last step of a call
+//   tA, tB     n  f32 heat scalar ping-pong (result always ends in tA)
+//   outlet_u   ny*nz float4: previous velocity of the outlet column x = nx-1
+//   tau0_x     nx f32: the x-dependent base relaxation time (sponges)
+//   scratch    force partial records of the pending steps + mass partials
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "../../include/wt.h"
+
+#define WT_HIST_CAP 16384u    // per-step force records kept on the device (ring)
+#define WT_PENDING_MAX 64u    // steps whose partials wait for one reduction launch
+
+namespace wt {
+
+// Per-block force partial of one step: FP64 sums (x,y,z per group) and the
+// reference's i32 fixed-point sums (x,y per group, wrapping).
+struct ForceSlot {
+  double f[9];
+  int32_t raw[6];
+};
+
+struct StepArgs {
+  void* pop;
+  const uint32_t* cellw;
+  const uint8_t* solid;
+  float4* fields;
+  float4* outlet_u;
+  const float* tau0_x;
+  const int32_t* block_slot;   // block -> slot or -1
+  ForceSlot* slots;            // this step's partial records [nslots]
+  double* mass_partial;        // [nblocks] (field steps only)
+  unsigned int* guard_count;
+  uint32_t nx, ny, nz;
+  uint64_t n, np;
+  float u_in, ks2;             // ks2 = (18*1.41421356 as f32) * smag * smag
+  float feq_in[19];            // feq(i, 1, (u_in, 0, 0))
+  float floor_k[19];           // 6 * w_i * c_ix (belt term coefficient)
+};
+
+struct HeatArgs {
+  const float4* fields;
+  const float* emit;
+  const float* tin;
+  float* tout;
+  uint32_t nx, ny, nz;
+  float dt, cool, diffuse, src_mix;
+};
+
+// Launch geometry of the step kernels.
+struct StepGeom {
+  dim3 block, grid;
+  uint32_t nblocks;
+};
+
+StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx);
+
+// wt_lbm.cu
+cudaError_t launch_init(uint32_t storage, void* pop, float4* fields, float4* outlet_u, uint32_t nx, uint32_t ny,
+                        uint32_t nz, uint64_t np, float u_in, cudaStream_t s);
+cudaError_t launch_step(uint32_t storage, bool gather, bool write_fields, const StepGeom& g, const StepArgs& a,
+                        cudaStream_t s);
+cudaError_t launch_force_reduce(const ForceSlot* slots, uint32_t nslots, uint32_t nsteps, double* hist,
+                                uint32_t hist_cap, uint64_t hist_base, double* totals, int32_t* raw_totals,
+                                const double* mass_partial, uint32_t nmass, double* mass_out, unsigned int* counter,
+                                cudaStream_t s);
+cudaError_t launch_read_pop(uint32_t storage, const void* pop, float* out, uint32_t n, uint64_t np, cudaStream_t s);
+cudaError_t launch_write_pop(uint32_t storage, const float* in, void* pop, uint32_t n, uint64_t np, cudaStream_t s);
+cudaError_t launch_resample_init(uint32_t storage, const float4* coarse, uint32_t cx, uint32_t cy, uint32_t cz,
+                                 void* pop, float4* fields, float4* outlet_u, uint32_t nx, uint32_t ny, uint32_t nz,
+                                 uint64_t np, cudaStream_t s);
+
+// wt_voxel.cu
+cudaError_t launch_voxelize(const wt_shape& shape, const wt_grid& grid, uint8_t* solid, float* emit,
+                            cudaStream_t s);
+cudaError_t launch_cell_words(const uint8_t* solid, const float* emit, uint32_t* cellw, uint32_t nx, uint32_t ny,
+                              uint32_t nz, cudaStream_t s);
+cudaError_t launch_block_flags(const uint32_t* cellw, const StepGeom& g, uint32_t nx, uint32_t ny, uint32_t nz,
+                               uint8_t* flags, cudaStream_t s);
+cudaError_t launch_links_out(const uint32_t* cellw, uint32_t* links, uint64_t n, cudaStream_t s);
+cudaError_t launch_solid_u32(const uint8_t* solid, uint32_t* out, uint64_t n, cudaStream_t s);
+cudaError_t launch_solid_from_u32(const uint32_t* in, uint8_t* solid, uint64_t n, cudaStream_t s);
+
+// wt_heat.cu
+cudaError_t launch_heat(const HeatArgs& a, cudaStream_t s);
+
+}  // namespace wt

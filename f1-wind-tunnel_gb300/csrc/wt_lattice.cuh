@@ -1,0 +1,77 @@
+// D3Q19 tables as compile-time functions, cell-word bits and the population
+// storage formats.  The velocity order, opposite and z-mirror permutations and
+// weights are those of the reference (src/engine/wgsl.ts:123-133); they are
+// restated as constexpr functions so that every per-direction branch folds away
+// inside the unrolled kernels.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include <utility>
+
+namespace wt {
+
+__host__ __device__ constexpr int CXd(int i) {
+  return (i == 1 || i == 7 || i == 9 || i == 11 || i == 13) ? 1 : (i == 2 || i == 8 || i == 10 || i == 12 || i == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int CYd(int i) {
+  return (i == 3 || i == 7 || i == 10 || i == 15 || i == 17) ? 1 : (i == 4 || i == 8 || i == 9 || i == 16 || i == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int CZd(int i) {
+  return (i == 5 || i == 11 || i == 14 || i == 15 || i == 18) ? 1 : (i == 6 || i == 12 || i == 13 || i == 16 || i == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int OPPd(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
+// Reflection z -> -z of direction i.
+__host__ __device__ constexpr int ZMIRd(int i) {
+  return i == 5 ? 6 : i == 6 ? 5 : i == 11 ? 13 : i == 13 ? 11 : i == 12 ? 14 : i == 14 ? 12
+       : i == 15 ? 17 : i == 17 ? 15 : i == 16 ? 18 : i == 18 ? 16 : i;
+}
+// Weights exactly as the reference's f32 literals.
+__host__ __device__ constexpr float Wd(int i) { return i == 0 ? 0.33333334f : (i < 7 ? 0.055555556f : 0.027777778f); }
+
+// Cell word (one u32 per cell, built at voxelization):
+//   bit 0      cell is solid
+//   bits 1-18  direction i of this fluid cell bounces back off a solid source
+//              cell (the `solid[sidx] != 0` branch of wgsl.ts:221, mirror included)
+//   bit 19     belt contact: floor speed 0 under this y=0 cell (wgsl.ts:192-197)
+//   bit 20     duct cell (emit < 0): no force, axial velocity relaxation (wgsl.ts:201,248)
+//   bit 21     at least one force-carrying link (non-mirrored, not a duct cell)
+constexpr uint32_t CW_SOLID = 1u;
+constexpr uint32_t CW_LINKS = 0x7fffeu;
+constexpr uint32_t CW_BELT = 1u << 19;
+constexpr uint32_t CW_DUCT = 1u << 20;
+constexpr uint32_t CW_FORCE = 1u << 21;
+
+// Compile-time loop: f(std::integral_constant<int, I>) for I = 0..N-1.
+template <int... Is, class F>
+__device__ __forceinline__ void sfor_impl(std::integer_sequence<int, Is...>, F&& f) {
+  (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void sfor(F&& f) {
+  sfor_impl(std::make_integer_sequence<int, N>{}, f);
+}
+
+// Population storage.  F32 keeps f_i; F16/BF16 keep f_i - w_i, which is small
+// and keeps the significant bits of the deviation from rest.
+struct StoreF32 {
+  typedef float T;
+  static constexpr uint32_t id = 0;
+  __device__ __forceinline__ static float ld(const T* p, float) { return __ldg(p); }
+  __device__ __forceinline__ static void st(T* p, float v, float) { *p = v; }
+  __host__ __device__ static float enc_host(float v, float) { return v; }
+};
+struct StoreF16 {
+  typedef __half T;
+  static constexpr uint32_t id = 1;
+  __device__ __forceinline__ static float ld(const T* p, float w) { return w + __half2float(__ldg(p)); }
+  __device__ __forceinline__ static void st(T* p, float v, float w) { *p = __float2half_rn(v - w); }
+};
+struct StoreBF16 {
+  typedef __nv_bfloat16 T;
+  static constexpr uint32_t id = 2;
+  __device__ __forceinline__ static float ld(const T* p, float w) { return w + __bfloat162float(__ldg(p)); }
+  __device__ __forceinline__ static void st(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
+};
+
+}  // namespace wt

@@ -1,0 +1,641 @@
+// D3Q19 regularized LBM with Smagorinsky LES: the collide-stream step of the
+// reference (LBM_STEP, src/engine/wgsl.ts:157-291) and its init (LBM_INIT,
+// wgsl.ts:141-155), as an in-place AA-pattern single lattice.
+//
+// Storage: one array per direction, pop[i*np + idx].  Two step kinds alternate:
+//   gather step  (odd steps 1, 3, ...): state C -> state S
+//       reads  f_i(x) = pop[opp(i)][x - c_i]           (neighbour slots)
+//       writes f*_j(x) -> pop[j][x + c_j]                (neighbour slots)
+//   local step   (even steps 2, 4, ...): state S -> state C
+//       reads  f_i(x) = pop[i][x]                        (own slots)
+//       writes f*_j(x) -> pop[opp(j)][x]                 (own slots)
+// State C ("canonical", after every even number of steps) holds the
+// post-collision populations f*_j(x) at pop[opp(j)][x] - the same information
+// as the reference's buffer fA after engine.ts:710's even-length loop - and
+// does not depend on the link masks, so re-voxelization between calls is exact.
+//
+// Boundaries keep the reference's precedence (wgsl.ts:207-227): inlet (x<0),
+// outlet (x>=nx, feq of the cell's previous velocity), moving floor (y<0,
+// bounce-back + 6 w c_x u_floor), far field (y>=ny or z>=nz), symmetry mirror
+// (z<0), solid bounce-back, interior.  In AA form the bounce-back, floor and
+// mirror values are redirected on write so that every read of the next step
+// finds its value: bounce-back/floor -> own slot pop[opp(j)][x]; mirror ->
+// pop[zmir(j)][(x + c_jx, y + c_jy, 0)].  Every slot written in a step is read
+// in that step only by the writing thread, so the step has no races.
+//
+// Arithmetic matches the reference operation for operation (no contraction,
+// compile with -fmad=false): sums run in the reference's direction order, and
+// only products with a zero lattice coefficient are dropped, which leaves every
+// finite result bit-identical.
+//
+// Roofline: 19 loads + 19 stores of the storage type + one 4-byte cell word per
+// cell and step (156 B/LUP in f32, 80 B/LUP in f16/bf16); the (u, rho) field
+// write (16 B) happens only on the last step of a call.
+#include "wt_internal.h"
+#include "wt_lattice.cuh"
+
+namespace wt {
+
+namespace {
+
+constexpr int BX_MAX = 256;
+
+struct CellOut {
+  float ux, uy, uz, rho;
+  bool guard;
+};
+
+// feq of wgsl.ts:135-138 with rho = 1 (outlet populations from the previous velocity).
+template <int i>
+__device__ __forceinline__ float feq_rho1(float ux, float uy, float uz) {
+  constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
+  float cu = 0.0f;
+  bool first = true;
+  if constexpr (cx != 0) { cu = (cx > 0) ? ux : -ux; first = false; }
+  if constexpr (cy != 0) { if (first) cu = (cy > 0) ? uy : -uy; else cu = (cy > 0) ? cu + uy : cu - uy; first = false; }
+  if constexpr (cz != 0) { if (first) cu = (cz > 0) ? uz : -uz; else cu = (cz > 0) ? cu + uz : cu - uz; }
+  const float uu = ux * ux + uy * uy + uz * uz;
+  return Wd(i) * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
+}
+
+// c_i . u with the reference's x, y, z order and zero terms dropped.
+template <int i>
+__device__ __forceinline__ float cdot(float ux, float uy, float uz) {
+  constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
+  float cu = 0.0f;
+  bool first = true;
+  if constexpr (cx != 0) { cu = (cx > 0) ? ux : -ux; first = false; }
+  if constexpr (cy != 0) { if (first) cu = (cy > 0) ? uy : -uy; else cu = (cy > 0) ? cu + uy : cu - uy; first = false; }
+  if constexpr (cz != 0) { if (first) cu = (cz > 0) ? uz : -uz; else cu = (cz > 0) ? cu + uz : cu - uz; }
+  return cu;
+}
+
+__device__ __forceinline__ bool is_bad(float x) { return (__float_as_uint(x) & 0x7f800000u) == 0x7f800000u; }
+
+// Moments, divergence guard, duct relaxation, regularized + Smagorinsky collision
+// (wgsl.ts:231-272).  f[] in, fo[] out.
+__device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19], float tau0, float u_in, float ks2,
+                                           bool duct) {
+  CellOut o;
+  float rho = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f;
+  sfor<19>([&](auto I) {
+    constexpr int i = I;
+    rho = rho + f[i];
+    if constexpr (CXd(i) > 0) mx = mx + f[i];
+    if constexpr (CXd(i) < 0) mx = mx - f[i];
+    if constexpr (CYd(i) > 0) my = my + f[i];
+    if constexpr (CYd(i) < 0) my = my - f[i];
+    if constexpr (CZd(i) > 0) mz = mz + f[i];
+    if constexpr (CZd(i) < 0) mz = mz - f[i];
+  });
+  const float den = (rho < 1e-4f) ? 1e-4f : rho;
+  float ux = mx / den, uy = my / den, uz = mz / den;
+  float g[19];
+  bool guard = is_bad(rho) || is_bad(ux) || is_bad(uy) || is_bad(uz) || rho < 0.3f || rho > 3.0f ||
+               __fsqrt_rn(ux * ux + uy * uy + uz * uz) > 0.35f;
+  if (guard) {
+    rho = 1.0f;
+    ux = u_in * 0.5f; uy = 0.0f; uz = 0.0f;
+    const float uu = ux * ux + uy * uy + uz * uz;
+    sfor<19>([&](auto I) {
+      constexpr int i = I;
+      const float cu = cdot<i>(ux, uy, uz);
+      g[i] = Wd(i) * rho * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
+    });
+  } else {
+    sfor<19>([&](auto I) { g[I] = f[I]; });
+  }
+  if (duct) {
+    const float t = 0.04f, tu = 1.0f - 0.04f;
+    ux = ux * tu + (0.55f * u_in) * t;
+    uy = uy * tu + uy * t;
+    uz = uz * tu + uz * t;
+  }
+  const float uu = ux * ux + uy * uy + uz * uz;
+  const float uu15 = 1.5f * uu;
+  const float wr0 = Wd(0) * rho, wr1 = Wd(1) * rho, wr2 = Wd(7) * rho;
+  float eq[19];
+  float pxx = 0.0f, pyy = 0.0f, pzz = 0.0f, pxy = 0.0f, pxz = 0.0f, pyz = 0.0f;
+  sfor<19>([&](auto I) {
+    constexpr int i = I;
+    constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
+    const float cu = cdot<i>(ux, uy, uz);
+    const float wr = (i == 0) ? wr0 : (i < 7 ? wr1 : wr2);
+    eq[i] = wr * (1.0f + 3.0f * cu + 4.5f * cu * cu - uu15);
+    const float ne = g[i] - eq[i];
+    if constexpr (cx != 0) pxx = pxx + ne;
+    if constexpr (cy != 0) pyy = pyy + ne;
+    if constexpr (cz != 0) pzz = pzz + ne;
+    if constexpr (cx * cy > 0) pxy = pxy + ne;
+    if constexpr (cx * cy < 0) pxy = pxy - ne;
+    if constexpr (cx * cz > 0) pxz = pxz + ne;
+    if constexpr (cx * cz < 0) pxz = pxz - ne;
+    if constexpr (cy * cz > 0) pyz = pyz + ne;
+    if constexpr (cy * cz < 0) pyz = pyz - ne;
+  });
+  const float q = __fsqrt_rn(pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
+  const float tau = 0.5f * (tau0 + __fsqrt_rn(tau0 * tau0 + __fdiv_rn(ks2 * q, rho)));
+  const float omega = __fdiv_rn(1.0f, tau);
+  const float c1 = (1.0f - omega) * 4.5f;
+  const float k0 = c1 * Wd(0), k1 = c1 * Wd(1), k2 = c1 * Wd(7);
+  // (c_a c_a - 1/3) with the reference's f32 third: 1 - third rounds to 0x1.555554p-1
+  constexpr float third = 0x1.555556p-2f;
+  const float a_xx = (1.0f - third) * pxx, b_xx = (0.0f - third) * pxx;
+  const float a_yy = (1.0f - third) * pyy, b_yy = (0.0f - third) * pyy;
+  const float a_zz = (1.0f - third) * pzz, b_zz = (0.0f - third) * pzz;
+  const float pxy2 = 2.0f * pxy, pxz2 = 2.0f * pxz, pyz2 = 2.0f * pyz;
+  sfor<19>([&](auto I) {
+    constexpr int i = I;
+    constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
+    float qp = ((cx != 0) ? a_xx : b_xx) + ((cy != 0) ? a_yy : b_yy);
+    qp = qp + ((cz != 0) ? a_zz : b_zz);
+    if constexpr (cx * cy > 0) qp = qp + pxy2;
+    if constexpr (cx * cy < 0) qp = qp - pxy2;
+    if constexpr (cx * cz > 0) qp = qp + pxz2;
+    if constexpr (cx * cz < 0) qp = qp - pxz2;
+    if constexpr (cy * cz > 0) qp = qp + pyz2;
+    if constexpr (cy * cz < 0) qp = qp - pyz2;
+    const float kw = (i == 0) ? k0 : (i < 7 ? k1 : k2);
+    fo[i] = eq[i] + kw * qp;
+  });
+  o.ux = ux; o.uy = uy; o.uz = uz; o.rho = rho; o.guard = guard;
+  return o;
+}
+
+template <class St>
+__device__ __forceinline__ float ldp(const void* pop, int dir, uint32_t np, uint32_t cell) {
+  return St::ld(reinterpret_cast<const typename St::T*>(pop) + (size_t)dir * np + cell, Wd(dir));
+}
+template <class St>
+__device__ __forceinline__ void stp(void* pop, int dir, uint32_t np, uint32_t cell, float v, int wdir) {
+  St::st(reinterpret_cast<typename St::T*>(pop) + (size_t)dir * np + cell, v, Wd(wdir));
+}
+
+// Momentum exchange of one force-carrying link (wgsl.ts:221-223): the bounced
+// value v = f[i]; group from the source cell's solid flag.
+template <int i>
+__device__ __forceinline__ void link_force(float v, uint32_t group, float (&gf)[9]) {
+  const float t = 2.0f * (v - Wd(i));
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    if (group == (uint32_t)(k + 1)) {
+      if constexpr (CXd(i) > 0) gf[3 * k] = gf[3 * k] - t;
+      if constexpr (CXd(i) < 0) gf[3 * k] = gf[3 * k] + t;
+      if constexpr (CYd(i) > 0) gf[3 * k + 1] = gf[3 * k + 1] - t;
+      if constexpr (CYd(i) < 0) gf[3 * k + 1] = gf[3 * k + 1] + t;
+      if constexpr (CZd(i) > 0) gf[3 * k + 2] = gf[3 * k + 2] - t;
+      if constexpr (CZd(i) < 0) gf[3 * k + 2] = gf[3 * k + 2] + t;
+    }
+  }
+}
+
+template <class St, bool GATHER, bool FIELDS>
+__global__ void __launch_bounds__(128) step_kernel(StepArgs a) {
+  const uint8_t* __restrict__ solid_u8 = a.solid;
+  const uint32_t nx = a.nx, ny = a.ny, nz = a.nz;
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+  const uint32_t z = blockIdx.z;
+  const bool in = (x < nx) && (y < ny);
+  const uint32_t nxy = nx * ny;
+  const uint32_t np = (uint32_t)a.np;
+  const uint32_t idx = in ? x + nx * y + nxy * z : 0u;
+  const uint32_t cw = in ? __ldg(a.cellw + idx) : CW_SOLID;
+  float gf[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float rho_cell = 0.0f;
+  bool guard = false;
+
+  if (in && (cw & CW_SOLID)) {
+    if constexpr (!GATHER) {  // wgsl.ts:183: solid cells hold w_i
+      sfor<19>([&](auto K) { stp<St>(a.pop, K, np, idx, Wd(K), K); });
+    }
+    if constexpr (FIELDS) a.fields[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+  } else if (in) {
+    const bool face = (x == 0) | (x == nx - 1) | (y == 0) | (y == ny - 1) | (z == 0) | (z == nz - 1);
+    float f[19], fo[19];
+    float4 pu = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (x == nx - 1) pu = a.outlet_u[y + ny * z];
+    const float floor_u = (cw & CW_BELT) ? 0.0f : a.u_in;
+
+    // ---------------------------------------------------------------- gather
+    if (!face) {
+      sfor<19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (i == 0) {
+          f[0] = ldp<St>(a.pop, 0, np, idx);
+        } else if constexpr (GATHER) {
+          constexpr int off_x = CXd(i), off_y = CYd(i), off_z = CZd(i);
+          const int off = off_x + off_y * (int)nx + off_z * (int)nxy;
+          const bool bb = (cw >> i) & 1u;
+          const uint32_t slot = bb ? (uint32_t)i * np + idx : (uint32_t)OPPd(i) * np + (uint32_t)((int)idx - off);
+          const int wdir = bb ? i : OPPd(i);
+          f[i] = St::ld(reinterpret_cast<const typename St::T*>(a.pop) + slot, Wd(wdir));
+        } else {
+          f[i] = ldp<St>(a.pop, i, np, idx);
+        }
+      });
+    } else {
+      sfor<19>([&](auto I) {
+        constexpr int i = I;
+        constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
+        if constexpr (i == 0) {
+          f[0] = ldp<St>(a.pop, 0, np, idx);
+        } else {
+          float v;
+          if (cx > 0 && x == 0) {
+            v = a.feq_in[i];
+          } else if (cx < 0 && x == nx - 1) {
+            v = feq_rho1<i>(pu.x, pu.y, pu.z);
+          } else if (cy > 0 && y == 0) {
+            v = ldp<St>(a.pop, i, np, idx);
+            if constexpr (cx != 0) v = v + a.floor_k[i] * floor_u;
+          } else if ((cy < 0 && y == ny - 1) || (cz < 0 && z == nz - 1)) {
+            v = a.feq_in[i];
+          } else if (GATHER) {
+            if ((cw >> i) & 1u) {
+              v = ldp<St>(a.pop, i, np, idx);
+            } else if (cz > 0 && z == 0) {
+              v = ldp<St>(a.pop, OPPd(ZMIRd(i)), np, (uint32_t)((int)idx - cx - cy * (int)nx));
+            } else {
+              const int off = cx + cy * (int)nx + cz * (int)nxy;
+              v = ldp<St>(a.pop, OPPd(i), np, (uint32_t)((int)idx - off));
+            }
+          } else {
+            v = ldp<St>(a.pop, i, np, idx);
+          }
+          f[i] = v;
+        }
+      });
+    }
+
+    // ---------------------------------------------------------------- forces
+    if (cw & CW_FORCE) {
+      sfor<19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (i != 0) {
+          constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
+          const bool mirrored = (cz > 0) && (z == 0);
+          if (((cw >> i) & 1u) && !mirrored) {
+            const int off = cx + cy * (int)nx + cz * (int)nxy;
+            const uint32_t grp = __ldg(solid_u8 + (uint32_t)((int)idx - off));
+            link_force<i>(f[i], grp, gf);
+          }
+        }
+      });
+    }
+
+    // ---------------------------------------------------------------- collide
+    const CellOut o = collide(f, fo, __ldg(a.tau0_x + x), a.u_in, a.ks2, (cw & CW_DUCT) != 0);
+    if (o.guard) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) gf[k] = 0.0f;
+    }
+    guard = o.guard;
+    rho_cell = o.rho;
+    if (x == nx - 1) a.outlet_u[y + ny * z] = make_float4(o.ux, o.uy, o.uz, 0.0f);
+    if constexpr (FIELDS) a.fields[idx] = make_float4(o.ux, o.uy, o.uz, o.rho);
+
+    // ---------------------------------------------------------------- scatter
+    if constexpr (!GATHER) {
+      sfor<19>([&](auto J) {
+        constexpr int j = J;
+        stp<St>(a.pop, OPPd(j), np, idx, fo[j], j);
+      });
+    } else if (!face) {
+      sfor<19>([&](auto J) {
+        constexpr int j = J;
+        if constexpr (j == 0) {
+          stp<St>(a.pop, 0, np, idx, fo[0], 0);
+        } else {
+          constexpr int i = OPPd(j);
+          const int off = CXd(j) + CYd(j) * (int)nx + CZd(j) * (int)nxy;
+          const bool bb = (cw >> i) & 1u;
+          const uint32_t slot = bb ? (uint32_t)i * np + idx : (uint32_t)j * np + (uint32_t)((int)idx + off);
+          St::st(reinterpret_cast<typename St::T*>(a.pop) + slot, fo[j], Wd(j));
+        }
+      });
+    } else {
+      sfor<19>([&](auto J) {
+        constexpr int j = J;
+        constexpr int cx = CXd(j), cy = CYd(j), cz = CZd(j);
+        constexpr int i = OPPd(j);
+        if constexpr (j == 0) {
+          stp<St>(a.pop, 0, np, idx, fo[0], 0);
+        } else {
+          if (cx < 0 && x == 0) {
+            // inlet side: the reference never reads this value
+          } else if (cx > 0 && x == nx - 1) {
+            // outlet side: discarded
+          } else if (cy < 0 && y == 0) {
+            stp<St>(a.pop, i, np, idx, fo[j], j);  // moving-floor bounce-back source
+          } else if ((cy > 0 && y == ny - 1) || (cz > 0 && z == nz - 1)) {
+            // far field: discarded
+          } else if ((cw >> i) & 1u) {
+            stp<St>(a.pop, i, np, idx, fo[j], j);  // bounce-back source (mirror included)
+          } else if (cz < 0 && z == 0) {
+            stp<St>(a.pop, ZMIRd(j), np, (uint32_t)((int)idx + cx + cy * (int)nx), fo[j], j);
+          } else {
+            const int off = cx + cy * (int)nx + cz * (int)nxy;
+            stp<St>(a.pop, j, np, (uint32_t)((int)idx + off), fo[j], j);
+          }
+        }
+      });
+    }
+  }
+
+  // -------------------------------------------------------------- reductions
+  const uint32_t lane = threadIdx.x & 31u, warp = (threadIdx.x + blockDim.x * threadIdx.y) >> 5;
+  const uint32_t nwarps = (blockDim.x * blockDim.y + 31) >> 5;
+  const uint32_t blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  const unsigned gb = __ballot_sync(0xffffffffu, guard);
+  if (gb && lane == 0) atomicAdd(a.guard_count, (unsigned)__popc(gb));
+
+  __shared__ double s_f[9][8];
+  __shared__ int32_t s_r[6][8];
+  __shared__ double s_m[8];
+  const int32_t slot = __ldg(a.block_slot + blk);
+  if (slot >= 0) {
+    double d[9];
+    int32_t r[6];
+#pragma unroll
+    for (int k = 0; k < 9; k++) d[k] = (double)gf[k];
+#pragma unroll
+    for (int g = 0; g < 3; g++) {
+      r[2 * g] = (gf[3 * g] != 0.0f) ? __float2int_rn(gf[3 * g] * 10000.0f) : 0;
+      r[2 * g + 1] = (gf[3 * g + 1] != 0.0f) ? __float2int_rn(gf[3 * g + 1] * 10000.0f) : 0;
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) d[k] += __shfl_down_sync(0xffffffffu, d[k], s);
+#pragma unroll
+      for (int k = 0; k < 6; k++) r[k] = (int32_t)((uint32_t)r[k] + (uint32_t)__shfl_down_sync(0xffffffffu, r[k], s));
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) s_f[k][warp] = d[k];
+#pragma unroll
+      for (int k = 0; k < 6; k++) s_r[k][warp] = r[k];
+    }
+  }
+  if constexpr (FIELDS) {
+    double m = (in && !(cw & CW_SOLID)) ? (double)rho_cell : 0.0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) m += __shfl_down_sync(0xffffffffu, m, s);
+    if (lane == 0) s_m[warp] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    if (slot >= 0) {
+      ForceSlot& out = a.slots[slot];
+      for (int k = 0; k < 9; k++) {
+        double t = 0.0;
+        for (uint32_t w = 0; w < nwarps; w++) t += s_f[k][w];
+        out.f[k] = t;
+      }
+      for (int k = 0; k < 6; k++) {
+        uint32_t t = 0;
+        for (uint32_t w = 0; w < nwarps; w++) t += (uint32_t)s_r[k][w];
+        out.raw[k] = (int32_t)t;
+      }
+    }
+    if constexpr (FIELDS) {
+      double t = 0.0;
+      for (uint32_t w = 0; w < nwarps; w++) t += s_m[w];
+      a.mass_partial[blk] = t;
+    }
+  }
+}
+
+// Canonical initial state (LBM_INIT, wgsl.ts:147-155): f*_j = feq_j(1, (u_in,0,0))
+// stored at pop[opp(j)][x] for every cell, fields (u_in,0,0,1).
+struct Feq19 {
+  float v[19];
+};
+
+template <class St>
+__global__ void init_kernel(void* pop, float4* fields, float4* outlet_u, uint32_t n, uint32_t ny, uint32_t nz,
+                            uint32_t np, float u_in, Feq19 feq_in) {
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < n) {
+    sfor<19>([&](auto J) { stp<St>(pop, OPPd(J), np, idx, feq_in.v[J], J); });
+    fields[idx] = make_float4(u_in, 0.0f, 0.0f, 1.0f);
+  }
+  if (idx < ny * nz) outlet_u[idx] = make_float4(u_in, 0.0f, 0.0f, 0.0f);
+}
+
+template <class St>
+__global__ void read_pop_kernel(const void* pop, float* out, uint32_t n, uint32_t np) {
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  sfor<19>([&](auto J) { out[(size_t)J * n + idx] = ldp<St>(pop, OPPd(J), np, idx) ; });
+}
+
+template <class St>
+__global__ void write_pop_kernel(const float* in, void* pop, uint32_t n, uint32_t np) {
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  sfor<19>([&](auto J) { stp<St>(pop, OPPd(J), np, idx, in[(size_t)J * n + idx], J); });
+}
+
+// Warm start: trilinear resample of a coarse (ux,uy,uz,rho) field onto the
+// lattice, populations set to feq(rho, u).
+template <class St>
+__global__ void resample_kernel(const float4* coarse, uint32_t cx, uint32_t cy, uint32_t cz, void* pop,
+                                float4* fields, float4* outlet_u, uint32_t nx, uint32_t ny, uint32_t nz,
+                                uint32_t np) {
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nx * ny * nz) return;
+  const uint32_t x = idx % nx, y = (idx / nx) % ny, z = idx / (nx * ny);
+  const float gx = ((float)x + 0.5f) * (float)cx / (float)nx - 0.5f;
+  const float gy = ((float)y + 0.5f) * (float)cy / (float)ny - 0.5f;
+  const float gz = ((float)z + 0.5f) * (float)cz / (float)nz - 0.5f;
+  const float fx = fminf(fmaxf(gx, 0.0f), (float)(cx - 1)), fy = fminf(fmaxf(gy, 0.0f), (float)(cy - 1)),
+              fz = fminf(fmaxf(gz, 0.0f), (float)(cz - 1));
+  const uint32_t x0 = (uint32_t)fx, y0 = (uint32_t)fy, z0 = (uint32_t)fz;
+  const uint32_t x1 = min(x0 + 1, cx - 1), y1 = min(y0 + 1, cy - 1), z1 = min(z0 + 1, cz - 1);
+  const float tx = fx - (float)x0, ty = fy - (float)y0, tz = fz - (float)z0;
+  auto at = [&](uint32_t a, uint32_t b, uint32_t c) { return coarse[a + cx * (b + cy * c)]; };
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  const uint32_t xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int ox = k & 1, oy = (k >> 1) & 1, oz = (k >> 2) & 1;
+    const float w = (ox ? tx : 1.f - tx) * (oy ? ty : 1.f - ty) * (oz ? tz : 1.f - tz);
+    const float4 v = at(xs[ox], ys[oy], zs[oz]);
+    acc.x += w * v.x; acc.y += w * v.y; acc.z += w * v.z; acc.w += w * v.w;
+  }
+  const float rho = acc.w > 0.3f ? acc.w : 1.0f;
+  const float uu = acc.x * acc.x + acc.y * acc.y + acc.z * acc.z;
+  sfor<19>([&](auto J) {
+    constexpr int j = J;
+    const float cu = cdot<j>(acc.x, acc.y, acc.z);
+    const float e = Wd(j) * rho * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
+    stp<St>(pop, OPPd(j), np, idx, e, j);
+  });
+  fields[idx] = make_float4(acc.x, acc.y, acc.z, rho);
+  if (x == nx - 1) outlet_u[y + ny * z] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+}
+
+// Deterministic reduction of the pending steps' partial records: one block per
+// step sums its slots in a fixed order and writes the step's record to the
+// history ring; the last block to finish folds the steps into the running
+// totals in step order.
+__global__ void force_reduce_kernel(const ForceSlot* slots, uint32_t nslots, uint32_t nsteps, double* hist,
+                                    uint32_t hist_cap, uint64_t hist_base, double* totals, int32_t* raw_totals,
+                                    const double* mass_partial, uint32_t nmass, double* mass_out,
+                                    unsigned int* counter) {
+  const uint32_t step = blockIdx.x;
+  const uint32_t t = threadIdx.x;
+  __shared__ double sd[256];
+  __shared__ uint32_t sr[256];
+  __shared__ bool last;
+  const ForceSlot* base = slots + (size_t)step * nslots;
+  double* rec = hist + ((hist_base + step) % hist_cap) * 16;
+  for (int k = 0; k < 15; k++) {
+    double acc = 0.0;
+    uint32_t racc = 0;
+    for (uint32_t s = t; s < nslots; s += blockDim.x) {
+      if (k < 9) acc += base[s].f[k];
+      else racc += (uint32_t)base[s].raw[k - 9];
+    }
+    sd[t] = acc;
+    sr[t] = racc;
+    __syncthreads();
+    for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (t < w) { sd[t] += sd[t + w]; sr[t] += sr[t + w]; }
+      __syncthreads();
+    }
+    if (t == 0) rec[k] = (k < 9) ? sd[0] : (double)(int32_t)sr[0];
+    __syncthreads();
+  }
+  if (step == nsteps - 1 && nmass > 0) {
+    double acc = 0.0;
+    for (uint32_t s = t; s < nmass; s += blockDim.x) acc += mass_partial[s];
+    sd[t] = acc;
+    __syncthreads();
+    for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (t < w) sd[t] += sd[t + w];
+      __syncthreads();
+    }
+    if (t == 0) *mass_out = sd[0];
+  }
+  __threadfence();
+  if (t == 0) last = (atomicAdd(counter, 1u) == nsteps - 1);
+  __syncthreads();
+  if (last && t == 0) {
+    __threadfence();
+    for (uint32_t s = 0; s < nsteps; s++) {
+      const double* r = hist + ((hist_base + s) % hist_cap) * 16;
+      for (int k = 0; k < 9; k++) totals[k] += r[k];
+      for (int g = 0; g < 3; g++) {
+        raw_totals[3 * g] = (int32_t)((uint32_t)raw_totals[3 * g] + (uint32_t)(int32_t)r[9 + 2 * g]);
+        raw_totals[3 * g + 1] = (int32_t)((uint32_t)raw_totals[3 * g + 1] + (uint32_t)(int32_t)r[10 + 2 * g]);
+      }
+    }
+    *counter = 0u;
+  }
+}
+
+template <class St>
+cudaError_t launch_step_t(bool gather, bool fields, const StepGeom& g, const StepArgs& a, cudaStream_t s) {
+  if (gather) {
+    if (fields) step_kernel<St, true, true><<<g.grid, g.block, 0, s>>>(a);
+    else step_kernel<St, true, false><<<g.grid, g.block, 0, s>>>(a);
+  } else {
+    if (fields) step_kernel<St, false, true><<<g.grid, g.block, 0, s>>>(a);
+    else step_kernel<St, false, false><<<g.grid, g.block, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+// Host copy of feq(i, 1, (u, 0, 0)) with the reference's operation order
+// (wgsl.ts:135-138); host float arithmetic without contraction gives the same
+// bits as the device.
+Feq19 feq_inlet(float u) {
+  Feq19 r;
+  for (int i = 0; i < 19; i++) {
+    const float cu = (float)CXd(i) * u + (float)CYd(i) * 0.0f + (float)CZd(i) * 0.0f;
+    const float uu = u * u + 0.0f * 0.0f + 0.0f * 0.0f;
+    r.v[i] = Wd(i) * 1.0f * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
+  }
+  return r;
+}
+
+template <class F>
+cudaError_t by_storage(uint32_t storage, F&& f) {
+  switch (storage) {
+    case WT_STORE_F32: return f(StoreF32());
+    case WT_STORE_F16: return f(StoreF16());
+    case WT_STORE_BF16: return f(StoreBF16());
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx) {
+  StepGeom g;
+  if (bx == 0 || bx > BX_MAX) bx = 128;
+  uint32_t by = 128 / bx;
+  if (by == 0) by = 1;
+  g.block = dim3(bx, by, 1);
+  g.grid = dim3((nx + bx - 1) / bx, (ny + by - 1) / by, nz);
+  g.nblocks = g.grid.x * g.grid.y * g.grid.z;
+  return g;
+}
+
+
+cudaError_t launch_init(uint32_t storage, void* pop, float4* fields, float4* outlet_u, uint32_t nx, uint32_t ny,
+                        uint32_t nz, uint64_t np, float u_in, cudaStream_t s) {
+  const uint32_t n = nx * ny * nz;
+  const uint32_t cover = n > ny * nz ? n : ny * nz;
+  const Feq19 fe = feq_inlet(u_in);
+  return by_storage(storage, [&](auto st) {
+    using St = decltype(st);
+    init_kernel<St><<<(cover + 255) / 256, 256, 0, s>>>(pop, fields, outlet_u, n, ny, nz, (uint32_t)np, u_in, fe);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_step(uint32_t storage, bool gather, bool write_fields, const StepGeom& g, const StepArgs& a,
+                        cudaStream_t s) {
+  return by_storage(storage, [&](auto st) { return launch_step_t<decltype(st)>(gather, write_fields, g, a, s); });
+}
+
+cudaError_t launch_force_reduce(const ForceSlot* slots, uint32_t nslots, uint32_t nsteps, double* hist,
+                                uint32_t hist_cap, uint64_t hist_base, double* totals, int32_t* raw_totals,
+                                const double* mass_partial, uint32_t nmass, double* mass_out, unsigned int* counter,
+                                cudaStream_t s) {
+  if (nsteps == 0) return cudaSuccess;
+  force_reduce_kernel<<<nsteps, 256, 0, s>>>(slots, nslots, nsteps, hist, hist_cap, hist_base, totals, raw_totals,
+                                             mass_partial, nmass, mass_out, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_read_pop(uint32_t storage, const void* pop, float* out, uint32_t n, uint64_t np, cudaStream_t s) {
+  return by_storage(storage, [&](auto st) {
+    read_pop_kernel<decltype(st)><<<(n + 255) / 256, 256, 0, s>>>(pop, out, n, (uint32_t)np);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_write_pop(uint32_t storage, const float* in, void* pop, uint32_t n, uint64_t np, cudaStream_t s) {
+  return by_storage(storage, [&](auto st) {
+    write_pop_kernel<decltype(st)><<<(n + 255) / 256, 256, 0, s>>>(in, pop, n, (uint32_t)np);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_resample_init(uint32_t storage, const float4* coarse, uint32_t cx, uint32_t cy, uint32_t cz,
+                                 void* pop, float4* fields, float4* outlet_u, uint32_t nx, uint32_t ny, uint32_t nz,
+                                 uint64_t np, cudaStream_t s) {
+  const uint32_t n = nx * ny * nz;
+  return by_storage(storage, [&](auto st) {
+    resample_kernel<decltype(st)><<<(n + 255) / 256, 256, 0, s>>>(coarse, cx, cy, cz, pop, fields, outlet_u, nx, ny,
+                                                                  nz, (uint32_t)np);
+    return cudaGetLastError();
+  });
+}
+
+}  // namespace wt

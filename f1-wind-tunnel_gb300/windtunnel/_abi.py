@@ -1,0 +1,120 @@
+"""ctypes view of libwt (include/wt.h).
+
+The structures mirror the C header field for field; `load()` opens the
+in-tree build (f1-wind-tunnel_gb300/_build/libwt.so).  There is no fallback:
+if the library is missing or the device is not an sm_103a GPU, calls fail with
+WindTunnelError.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libwt.so")
+
+WT_OK = 0
+ERRORS = {
+    -1: "WT_ERR_ARG",
+    -2: "WT_ERR_CUDA",
+    -3: "WT_ERR_NOMEM",
+    -4: "WT_ERR_UNSUPPORTED",
+    -5: "WT_ERR_STATE",
+    -6: "WT_ERR_DEVICE",
+}
+STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
+STORAGE = {"f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
+KIND_F1, KIND_SPHERE, KIND_CUBE, KIND_WING, KIND_EMPTY, KIND_BOX = 0, 1, 2, 3, 6, 7
+
+
+class WindTunnelError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_uint32), ("ny", ctypes.c_uint32), ("nz", ctypes.c_uint32),
+                ("origin", ctypes.c_float * 3), ("h", ctypes.c_float)]
+
+
+class Sim(ctypes.Structure):
+    _fields_ = [("u_in", ctypes.c_float), ("tau0", ctypes.c_float), ("smag", ctypes.c_float),
+                ("sponge_cells", ctypes.c_float), ("sponge_amp", ctypes.c_float),
+                ("inlet_cells", ctypes.c_float), ("inlet_amp", ctypes.c_float),
+                ("heat_cool", ctypes.c_float), ("heat_diffuse", ctypes.c_float), ("heat_src_mix", ctypes.c_float),
+                ("storage", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Shape(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("profile_mode", ctypes.c_uint32), ("pw", ctypes.c_uint32),
+                ("ph", ctypes.c_uint32),
+                ("front_flap", ctypes.c_float), ("rear_main", ctypes.c_float), ("rear_flap", ctypes.c_float),
+                ("ride_h", ctypes.c_float),
+                ("aoa", ctypes.c_float), ("width", ctypes.c_float), ("axis_y", ctypes.c_float),
+                ("p_scale", ctypes.c_float),
+                ("p_origin", ctypes.c_float * 2), ("heat_brakes", ctypes.c_float), ("heat_engine", ctypes.c_float),
+                ("heat_rad", ctypes.c_float), ("front_wing", ctypes.c_float), ("rear_wing", ctypes.c_float),
+                ("sidepod", ctypes.c_float),
+                ("cover", ctypes.c_float), ("nose", ctypes.c_float), ("rear_ride", ctypes.c_float),
+                ("duct", ctypes.c_float),
+                ("box_center", ctypes.c_float * 3), ("box_half", ctypes.c_float * 3)]
+
+
+class Forces(ctypes.Structure):
+    _fields_ = [("raw", ctypes.c_int32 * 12), ("sum", ctypes.c_double * 9), ("mass", ctypes.c_double),
+                ("steps", ctypes.c_uint64), ("guarded", ctypes.c_uint64)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("cells", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("steps_total", ctypes.c_uint64),
+                ("storage", ctypes.c_uint32), ("fluid_cells", ctypes.c_uint32), ("solid_cells", ctypes.c_uint32 * 3),
+                ("boundary_blocks", ctypes.c_uint32), ("history_capacity", ctypes.c_uint32),
+                ("sm_count", ctypes.c_uint32)]
+
+
+_vp = ctypes.c_void_p
+_PROTOS = {
+    "wt_create": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(Sim), ctypes.POINTER(_vp)]),
+    "wt_destroy": (ctypes.c_int, [_vp]),
+    "wt_set_sim": (ctypes.c_int, [_vp, ctypes.POINTER(Sim)]),
+    "wt_reset": (ctypes.c_int, [_vp]),
+    "wt_voxelize": (ctypes.c_int, [_vp, ctypes.POINTER(Shape)]),
+    "wt_set_solid": (ctypes.c_int, [_vp, _vp, _vp]),
+    "wt_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+    "wt_read_forces": (ctypes.c_int, [_vp, ctypes.POINTER(Forces), ctypes.c_int]),
+    "wt_read_force_history": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32]),
+    "wt_read_fields": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "wt_read_populations": (ctypes.c_int, [_vp, _vp]),
+    "wt_write_state": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "wt_reset_from": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]),
+    "wt_info_get": (ctypes.c_int, [_vp, ctypes.POINTER(Info)]),
+    "wt_stream": (_vp, [_vp]),
+    "wt_sync": (ctypes.c_int, [_vp]),
+    "wt_last_error": (ctypes.c_char_p, [_vp]),
+    "wt_version": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(path=None):
+    """Open libwt.so and declare the prototypes.  Raises if it is not built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise WindTunnelError(-6, f"{p} is missing: build it with `python f1-wind-tunnel_gb300/build.py`")
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(lib, ctx, rc, what):
+    if rc != WT_OK:
+        msg = lib.wt_last_error(ctx)
+        raise WindTunnelError(rc, f"{what}: {msg.decode() if msg else ''}")

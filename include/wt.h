@@ -1,0 +1,198 @@
+/*
+ * libwt - GB300 (sm_103a) wind-tunnel simulation core, C ABI.
+ *
+ * Drop-in for the simulation half of the reference engine class
+ * `AeroEngine` (src/engine/engine.ts:159-769).  A TypeScript host binds these
+ * entry points through N-API/FFI in place of its WGSL dispatches; every other
+ * caller (Python ctypes, C, C++) uses them the same way.
+ *
+ * Conventions (all entry points):
+ *   - return 0 (WT_OK) on success, a negative WT_ERR_* code on failure;
+ *     wt_last_error(ctx) gives a one-line message for the last failure;
+ *   - the library owns all device memory of a context; callers pass plain
+ *     host structs and host buffers of the documented sizes;
+ *   - one context = one CUDA stream on the current device; calls on one context
+ *     must be serialised by the caller, different contexts are independent;
+ *   - there is no CPU fallback: without a usable sm_103a device wt_create fails.
+ *
+ * Lattice layout and conventions follow the reference shaders
+ * (src/engine/wgsl.ts:123-139): D3Q19 velocity order
+ *   0 rest; 1,2 +-x; 3,4 +-y; 5,6 +-z; 7..10 xy diagonals (1,1),(-1,-1),(1,-1),(-1,1);
+ *   11..14 xz; 15..18 yz;
+ * cell index idx = x + nx*(y + ny*z); x streamwise, y up (moving floor at y=0),
+ * z lateral with the symmetry plane at z=0 (half tunnel, z >= 0).
+ */
+#ifndef WT_H
+#define WT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WT_OK 0
+#define WT_ERR_ARG (-1)         /* invalid argument or size */
+#define WT_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define WT_ERR_NOMEM (-3)       /* device allocation failed */
+#define WT_ERR_UNSUPPORTED (-4) /* scene kind or option not built */
+#define WT_ERR_STATE (-5)       /* call not valid in the current state */
+#define WT_ERR_DEVICE (-6)      /* no sm_103a device / wrong architecture */
+
+/* Population storage format (see wt_sim.storage). */
+#define WT_STORE_F32 0u  /* f_i as float: 19*4 B per cell */
+#define WT_STORE_F16 1u  /* f_i - w_i as IEEE half: 19*2 B per cell */
+#define WT_STORE_BF16 2u /* f_i - w_i as bfloat16: 19*2 B per cell */
+
+/* Scene kinds, Shape.kind of src/engine/engine.ts:30 plus one build extension. */
+#define WT_KIND_F1 0u     /* analytic generic F1, src/engine/f1.ts:283-320 */
+#define WT_KIND_SPHERE 1u /* wgsl.ts:104 */
+#define WT_KIND_CUBE 2u   /* wgsl.ts:105, 1 m rounded cube at (2.6, 1.0, 0) */
+#define WT_KIND_WING 3u   /* wgsl.ts:106 */
+#define WT_KIND_EMPTY 6u  /* wgsl.ts:108 */
+#define WT_KIND_BOX 7u    /* build extension: axis-aligned box box_center +- box_half */
+
+/* Grid of one lattice: AeroEngine constructor fields dims/h/origin (engine.ts:226-231). */
+typedef struct wt_grid {
+  uint32_t nx, ny, nz; /* cells; nx >= 8, ny >= 2, nz >= 2 */
+  float origin[3];     /* world position of the corner of cell (0,0,0), metres */
+  float h;             /* cell size, metres */
+} wt_grid;
+
+/* Simulation parameters: the Sim uniform (wgsl.ts:158, engine.ts:249) plus the
+ * constants the reference hard-codes in its collision and heat shaders. */
+typedef struct wt_sim {
+  float u_in;          /* inlet speed, lattice units (engine.ts:110: 0.0925) */
+  float tau0;          /* base relaxation time (engine.ts:249: 0.508) */
+  float smag;          /* Smagorinsky constant Cs (engine.ts:249: 0.17) */
+  float sponge_cells;  /* outlet sponge ramp smoothstep(nx-cells, nx-1, x) (wgsl.ts:260: 18) */
+  float sponge_amp;    /* tau added at the outlet (0.4) */
+  float inlet_cells;   /* inlet ramp smoothstep(0, cells, x) (10) */
+  float inlet_amp;     /* tau added at the inlet (0.25) */
+  float heat_cool;     /* heat uniform cool (engine.ts:263: 0.004) */
+  float heat_diffuse;  /* heat uniform diffuse (0.04) */
+  float heat_src_mix;  /* source blend (wgsl.ts:508: 0.35) */
+  uint32_t storage;    /* WT_STORE_* (fixed at wt_create) */
+  uint32_t reserved;   /* must be 0 */
+} wt_sim;
+
+/* Scene description: the Shape uniform (wgsl.ts:9-18) word for word, angles in
+ * radians as engine.ts:429-448 packs them, followed by the box extension. */
+typedef struct wt_shape {
+  uint32_t kind, profile_mode, pw, ph;
+  float front_flap, rear_main, rear_flap, ride_h;
+  float aoa, width, axis_y, p_scale;
+  float p_origin[2], heat_brakes, heat_engine;
+  float heat_rad, front_wing, rear_wing, sidepod;
+  float cover, nose, rear_ride, duct;
+  float box_center[3], box_half[3]; /* WT_KIND_BOX only */
+} wt_shape;
+
+/* Force readout (engine.ts:739-761 maybeReadForces).  Groups g: 0 body, 1 front
+ * wing, 2 rear wing (solid flag values 1, 2, 3). */
+typedef struct wt_forces {
+  int32_t raw[12];     /* the reference's i32 accumulator, bit-compatible: raw[3g+0] = x,
+                          raw[3g+1] = y of round(1e4 * per-cell force), summed with wrap */
+  double sum[9];       /* the same per-cell forces summed in FP64 on the device:
+                          sum[3g+c], c = x, y, z (lattice units, momentum per step) */
+  double mass;         /* FP64 sum of rho over fluid cells after the last step */
+  uint64_t steps;      /* LBM steps accumulated since the last reset of the readout */
+  uint64_t guarded;    /* cells reset by the divergence guard since that reset */
+} wt_forces;
+
+/* Sizes and state of a context. */
+typedef struct wt_info {
+  uint64_t cells;          /* nx*ny*nz */
+  uint64_t device_bytes;   /* device memory held by the context */
+  uint64_t steps_total;    /* LBM steps since wt_reset */
+  uint32_t storage;        /* WT_STORE_* */
+  uint32_t fluid_cells;    /* after the last voxelization */
+  uint32_t solid_cells[3]; /* per group */
+  uint32_t boundary_blocks;/* step-kernel blocks that carry bounce-back links */
+  uint32_t history_capacity; /* per-step force records kept (ring) */
+  uint32_t sm_count;
+} wt_info;
+
+typedef struct wt_ctx wt_ctx;
+
+/* new AeroEngine(...) (engine.ts:226-345): allocate one lattice on the current device.
+ * The lattice starts in the reset state with an empty scene. */
+int wt_create(const wt_grid* grid, const wt_sim* sim, wt_ctx** out);
+
+/* Release everything the context holds.  Safe on NULL. */
+int wt_destroy(wt_ctx* ctx);
+
+/* syncSim (engine.ts:497-501): update the simulation parameters between steps.
+ * sim->storage must equal the value given to wt_create. */
+int wt_set_sim(wt_ctx* ctx, const wt_sim* sim);
+
+/* reset() (engine.ts:371-381, LBM_INIT wgsl.ts:147-155): populations to
+ * feq(1, (u_in,0,0)), fields to (u_in,0,0,1), temperatures to 0.  Keeps the scene. */
+int wt_reset(wt_ctx* ctx);
+
+/* setShape() (engine.ts:426-470, VOXELIZE wgsl.ts:305-321): voxelize the scene
+ * into solid flags, heat emission and bounce-back link masks.  Populations are
+ * kept (re-voxelize semantics, engine.ts:469). */
+int wt_voxelize(wt_ctx* ctx, const wt_shape* shape);
+
+/* Load externally computed flags instead of a scene: solid[n] in {0,1,2,3} and
+ * emit[n] (heat source in solid cells, negative marks a duct cell). */
+int wt_set_solid(wt_ctx* ctx, const uint32_t* solid, const float* emit);
+
+/* The compute pass of frame() (engine.ts:708-712): n_lbm_steps collide-stream
+ * steps (must be even and >= 2, as engine.ts:585 makes them), then heat_passes
+ * semi-Lagrangian heat passes (0 or an even number; engine.ts:711-712 issues 2)
+ * with backtrace time heat_dt (engine.ts:659-660 uses n_lbm_steps/2; pass <= 0
+ * for that default).  Asynchronous on the context stream. */
+int wt_step(wt_ctx* ctx, int n_lbm_steps, int heat_passes, float heat_dt);
+
+/* maybeReadForces (engine.ts:739-761): copy the force accumulators to *out and,
+ * if reset != 0, zero them (engine.ts:747).  Synchronises the context stream. */
+int wt_read_forces(wt_ctx* ctx, wt_forces* out, int reset);
+
+/* Per-step FP64 force records of the last `count` steps, oldest first:
+ * out[9*k + 3g + c].  count <= min(steps recorded, history_capacity). */
+int wt_read_force_history(wt_ctx* ctx, double* out, uint32_t count);
+
+/* debugRead() (engine.ts:763-768): any pointer may be NULL.
+ *   u_rho[4n]  (ux, uy, uz, rho) after the last step (0 in solid cells)
+ *   solid[n]   0 fluid, 1 body, 2 front wing, 3 rear wing
+ *   temps[n]   heat scalar after the last heat pass
+ *   emit[n]    heat source field from the voxelizer
+ *   links[n]   bit i (1..18) set when direction i of a fluid cell bounces back
+ *              off a solid neighbour (the branch wgsl.ts:221 takes), bit 19 set
+ *              for floor cells under a belt contact patch (wgsl.ts:192-197). */
+int wt_read_fields(wt_ctx* ctx, float* u_rho, uint32_t* solid, float* temps, float* emit, uint32_t* links);
+
+/* Post-collision populations in the reference's buffer order f[i*n + idx]
+ * (what fA holds after an even number of steps), converted to float. */
+int wt_read_populations(wt_ctx* ctx, float* f);
+
+/* Replace the state: populations f[19n] (post-collision, reference order),
+ * optional u_rho[4n] (fields, also the outlet's previous velocity) and temps[n]. */
+int wt_write_state(wt_ctx* ctx, const float* f, const float* u_rho, const float* temps);
+
+/* Warm start: set populations to feq(rho, u) of a coarse (ux,uy,uz,rho) field
+ * u_rho[4*cx*cy*cz] trilinearly resampled to the lattice; fields likewise. */
+int wt_reset_from(wt_ctx* ctx, const float* u_rho, uint32_t cx, uint32_t cy, uint32_t cz);
+
+int wt_info_get(wt_ctx* ctx, wt_info* out);
+
+/* The context's cudaStream_t (as void*), for callers that time or order work. */
+void* wt_stream(wt_ctx* ctx);
+
+/* Block until all work queued on the context has finished. */
+int wt_sync(wt_ctx* ctx);
+
+/* Message of the last failure on ctx (or of the last failed wt_create if ctx is NULL). */
+const char* wt_last_error(const wt_ctx* ctx);
+
+/* Library version, e.g. "libwt 0.1 sm_103a". */
+const char* wt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WT_H */

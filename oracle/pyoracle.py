@@ -1,0 +1,229 @@
+"""TEST INFRASTRUCTURE ONLY - ctypes wrappers of the oracle (oracle/_build/liboracle.so)
+and, where it was built, of the translated reference shaders (oracle/_ref/libwgslref.so).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libwgslref.so")
+REF_SRC = os.path.join(HERE, "_ref", "wgsl_modules.inc")
+_vp = ctypes.c_void_p
+_F = ctypes.c_float
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", HERE, "_build/liboracle.so"], check=True)
+    return ORACLE_SO
+
+
+def build_ref():
+    """Compile the translated reference if its generated source is present."""
+    if os.path.exists(REF_SRC) or os.path.isdir("/root/reference"):
+        r = subprocess.run(["make", "-s", "-C", HERE, "ref"], capture_output=True, text=True)
+        return os.path.exists(REF_SO) and r.returncode == 0
+    return False
+
+
+def _load_oracle():
+    if not os.path.exists(ORACLE_SO):
+        build_oracle()
+    L = ctypes.CDLL(ORACLE_SO)
+    L.wto_new.restype = _vp
+    L.wto_new.argtypes = [ctypes.c_int] * 3 + [_F] * 4 + [ctypes.c_int]
+    L.wto_free.argtypes = [_vp]
+    L.wto_set_params.argtypes = [_vp, _vp]
+    L.wto_reset.argtypes = [_vp]
+    L.wto_voxelize.argtypes = [_vp, _vp]
+    L.wto_set_solid.argtypes = [_vp, _vp, _vp]
+    L.wto_steps.argtypes = [_vp, ctypes.c_int]
+    L.wto_heat.argtypes = [_vp, _F]
+    L.wto_read.argtypes = [_vp] + [_vp] * 7 + [ctypes.c_int]
+    L.wto_read64.argtypes = [_vp, _vp, _vp]
+    L.wto_write_state.argtypes = [_vp, _vp, _vp, _vp]
+    L.wto_link_mask.argtypes = [_vp, _vp]
+    L.wto_guarded.restype = ctypes.c_uint64
+    L.wto_guarded.argtypes = [_vp]
+    L.wto_threads.restype = ctypes.c_int
+    L.wto_set_threads.argtypes = [ctypes.c_int]
+    return L
+
+
+def _load_ref():
+    if not os.path.exists(REF_SO) and not build_ref():
+        return None
+    L = ctypes.CDLL(REF_SO)
+    L.wtr_new.restype = _vp
+    L.wtr_new.argtypes = [ctypes.c_int] * 3 + [_F] * 4
+    L.wtr_free.argtypes = [_vp]
+    L.wtr_set_sim.argtypes = [_vp, _F, _F, _F]
+    L.wtr_set_heat.argtypes = [_vp, _F, _F]
+    L.wtr_reset.argtypes = [_vp]
+    L.wtr_voxelize.argtypes = [_vp, _vp]
+    L.wtr_set_solid.argtypes = [_vp, _vp, _vp]
+    L.wtr_steps.argtypes = [_vp, ctypes.c_int]
+    L.wtr_heat.argtypes = [_vp, _F]
+    L.wtr_read.argtypes = [_vp] + [_vp] * 6 + [ctypes.c_int]
+    L.wtr_write_state.argtypes = [_vp, _vp, _vp, _vp]
+    L.wtr_threads.restype = ctypes.c_int
+    return L
+
+
+_O = None
+_R = None
+
+
+def oracle_lib():
+    global _O
+    if _O is None:
+        _O = _load_oracle()
+    return _O
+
+
+def ref_lib():
+    global _R
+    if _R is None:
+        _R = _load_ref()
+    return _R
+
+
+def shape_words(shape) -> np.ndarray:
+    """The 30 32-bit words of a wt_shape (ctypes struct) as uint32."""
+    return np.frombuffer(bytes(shape), dtype=np.uint32).copy()
+
+
+class Oracle:
+    """CPU restatement of the tunnel path (wt_oracle.hpp); fp64=True gives the FP64 model."""
+
+    def __init__(self, dims, origin, h, sim=None, fp64=False):
+        self.L = oracle_lib()
+        self.dims = tuple(int(d) for d in dims)
+        self.n = int(np.prod(self.dims))
+        self.h = float(h)
+        self.p = self.L.wto_new(*self.dims, float(origin[0]), float(origin[1]), float(origin[2]), float(h),
+                                1 if fp64 else 0)
+        if sim is not None:
+            self.set_sim(sim)
+
+    def set_sim(self, sim):
+        prm = np.array([sim.u_in, sim.tau0, sim.smag, sim.sponge_cells, sim.sponge_amp, sim.inlet_cells,
+                        sim.inlet_amp, sim.heat_cool, sim.heat_diffuse, sim.heat_src_mix], np.float32)
+        self.L.wto_set_params(self.p, prm.ctypes.data)
+
+    def reset(self):
+        self.L.wto_reset(self.p)
+
+    def voxelize(self, shape):
+        w = shape_words(shape)
+        self.L.wto_voxelize(self.p, w.ctypes.data)
+
+    def set_solid(self, solid, emit):
+        s = np.ascontiguousarray(solid, np.uint32)
+        e = np.ascontiguousarray(emit, np.float32)
+        self.L.wto_set_solid(self.p, s.ctypes.data, e.ctypes.data)
+
+    def steps(self, n):
+        self.L.wto_steps(self.p, int(n))
+
+    def heat(self, dt):
+        self.L.wto_heat(self.p, float(dt))
+
+    def frame(self, steps=8, heat_passes=2):
+        self.steps(steps)
+        if heat_passes:
+            assert heat_passes == 2
+            self.heat(steps / 2.0)
+
+    def read(self, reset_forces=False):
+        n = self.n
+        out = dict(fields=np.zeros((n, 4), np.float32), solid=np.zeros(n, np.uint32), emit=np.zeros(n, np.float32),
+                   temps=np.zeros(n, np.float32), f=np.zeros(19 * n, np.float32), forces=np.zeros(12, np.int32),
+                   forces64=np.zeros(9, np.float64))
+        self.L.wto_read(self.p, out["fields"].ctypes.data, out["solid"].ctypes.data, out["emit"].ctypes.data,
+                        out["temps"].ctypes.data, out["f"].ctypes.data, out["forces"].ctypes.data,
+                        out["forces64"].ctypes.data, 1 if reset_forces else 0)
+        return out
+
+    def read64(self):
+        fields = np.zeros((self.n, 4), np.float64)
+        f = np.zeros(19 * self.n, np.float64)
+        self.L.wto_read64(self.p, fields.ctypes.data, f.ctypes.data)
+        return fields, f
+
+    def write_state(self, f=None, fields=None, temps=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (f, fields, temps)]
+        self.L.wto_write_state(self.p, *[None if a is None else a.ctypes.data for a in arrs])
+
+    def link_mask(self):
+        m = np.zeros(self.n, np.uint32)
+        self.L.wto_link_mask(self.p, m.ctypes.data)
+        return m
+
+    def guarded(self):
+        return int(self.L.wto_guarded(self.p))
+
+    def __del__(self):
+        try:
+            self.L.wto_free(self.p)
+        except Exception:
+            pass
+
+
+class Reference:
+    """The reference's own WGSL shaders compiled as C++ (oracle/_ref), f32 only."""
+
+    def __init__(self, dims, origin, h, sim=None):
+        self.L = ref_lib()
+        if self.L is None:
+            raise RuntimeError("oracle/_ref was not built (needs the reference checkout)")
+        self.dims = tuple(int(d) for d in dims)
+        self.n = int(np.prod(self.dims))
+        self.p = self.L.wtr_new(*self.dims, float(origin[0]), float(origin[1]), float(origin[2]), float(h))
+        if sim is not None:
+            self.L.wtr_set_sim(self.p, sim.u_in, sim.tau0, sim.smag)
+            self.L.wtr_set_heat(self.p, sim.heat_cool, sim.heat_diffuse)
+
+    def reset(self):
+        self.L.wtr_reset(self.p)
+
+    def voxelize(self, shape):
+        w = shape_words(shape)[:24].copy()
+        self.L.wtr_voxelize(self.p, w.ctypes.data)
+
+    def set_solid(self, solid, emit):
+        s = np.ascontiguousarray(solid, np.uint32)
+        e = np.ascontiguousarray(emit, np.float32)
+        self.L.wtr_set_solid(self.p, s.ctypes.data, e.ctypes.data)
+
+    def steps(self, n):
+        self.L.wtr_steps(self.p, int(n))
+
+    def heat(self, dt):
+        self.L.wtr_heat(self.p, float(dt))
+
+    def frame(self, steps=8, heat_passes=2):
+        self.steps(steps)
+        if heat_passes:
+            self.heat(steps / 2.0)
+
+    def read(self, reset_forces=False):
+        n = self.n
+        out = dict(fields=np.zeros((n, 4), np.float32), solid=np.zeros(n, np.uint32), emit=np.zeros(n, np.float32),
+                   temps=np.zeros(n, np.float32), f=np.zeros(19 * n, np.float32), forces=np.zeros(12, np.int32))
+        self.L.wtr_read(self.p, out["fields"].ctypes.data, out["solid"].ctypes.data, out["emit"].ctypes.data,
+                        out["temps"].ctypes.data, out["f"].ctypes.data, out["forces"].ctypes.data,
+                        1 if reset_forces else 0)
+        return out
+
+    def write_state(self, f=None, fields=None, temps=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (f, fields, temps)]
+        self.L.wtr_write_state(self.p, *[None if a is None else a.ctypes.data for a in arrs])
+
+    def __del__(self):
+        try:
+            self.L.wtr_free(self.p)
+        except Exception:
+            pass

@@ -38,7 +38,7 @@ static inline i32 to_i32(u32 x) { return (i32)x; }
 static inline i32 to_i32(bool x) { return x ? 1 : 0; }
 static inline i32 to_i32(f32 x) {
   if (!(x == x)) return 0;
-  if (x >= 2147483520.0f) return 2147483647;
+  if (x >= 2147483648.0f) return 2147483647;
   if (x <= -2147483648.0f) return (i32)0x80000000u;
   return (i32)x;
 }
@@ -48,7 +48,7 @@ static inline u32 to_u32(bool x) { return x ? 1u : 0u; }
 static inline u32 to_u32(f32 x) {
   if (!(x == x)) return 0u;
   if (x <= 0.0f) return 0u;
-  if (x >= 4294967040.0f) return 4294967295u;
+  if (x >= 4294967296.0f) return 4294967295u;
   return (u32)x;
 }
 template <class T> struct conv;

@@ -42,13 +42,13 @@ static inline float fsmooth_w(float lo, float hi, float x) {
 static inline float fsqrt_w(float x) { return __builtin_sqrtf(x); }
 static inline int32_t f2i_w(float x) {  // truncate toward zero, saturate, NaN -> 0
   if (!(x == x)) return 0;
-  if (x >= 2147483520.0f) return 2147483647;
+  if (x >= 2147483648.0f) return 2147483647;
   if (x <= -2147483648.0f) return (int32_t)0x80000000u;
   return (int32_t)x;
 }
 static inline uint32_t f2u_w(float x) {
   if (!(x == x) || x <= 0.0f) return 0u;
-  if (x >= 4294967040.0f) return 4294967295u;
+  if (x >= 4294967296.0f) return 4294967295u;
   return (uint32_t)x;
 }
 

@@ -1,0 +1,57 @@
+"""Shared helpers of the tests: replaying the golden scripts on the oracle or on libwt."""
+import hashlib
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def shape_from_dict(d):
+    from windtunnel import _abi
+    s = _abi.Shape()
+    for name, _ in s._fields_:
+        v = d[name]
+        if isinstance(v, list):
+            arr = getattr(s, name)
+            for k, x in enumerate(v):
+                arr[k] = x
+        else:
+            setattr(s, name, v)
+    return s
+
+
+def golden_shapes(man):
+    return {name: shape_from_dict(c["shape"]) for name, c in man["vox"].items()}
+
+
+def corrupt(f, n, cells):
+    f = f.copy()
+    cells = np.asarray(cells)
+    f[3 * n + cells[:4]] = np.nan
+    f[1 * n + cells[4:8]] = 50.0
+    f[7 * n + cells[8:]] = -40.0
+    return f
+
+
+def replay(sim_obj, man, case, read):
+    """Run the golden script of `case` on an object with voxelize/frame/read/write_state.
+    `read()` returns dict(fields, f, temps, forces).  Yields (frame_index, data)."""
+    rec = man["lbm"][case]
+    shapes = golden_shapes(man)
+    k = 0
+    for item in rec["script"]:
+        if item[0] == "shape":
+            sim_obj.voxelize(shapes[item[1]])
+        elif item[0] == "corrupt":
+            d = read()
+            n = d["fields"].shape[0]
+            sim_obj.write_state(f=corrupt(d["f"], n, item[2]))
+        else:
+            sim_obj.frame(item[1])
+            yield k, read()
+            k += 1
