@@ -189,6 +189,8 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=64, help="LBM steps per kernel-timing launch batch")
+    ap.add_argument("--profile", action="store_true",
+                    help="warm-up and timed frames only (for ncu captures); prints a short line")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -258,6 +260,13 @@ def main():
     total_cells = n * world
     value = total_cells * lbm_per_frame * frames / (ms / 1e3) / 1e6
     fr = eng.read_forces_raw()
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_frames": frames, "ms": ms, "mlups": value}), flush=True)
+        eng.close()
+        if dist:
+            dist.destroy_process_group()
+        return
     if fr.guarded:
         print(f"warning: {fr.guarded} cells hit the divergence guard", file=sys.stderr)
     launches_per_frame = lbm_per_frame + (lbm_per_frame + 63) // 64 + 2
