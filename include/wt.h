@@ -191,6 +191,32 @@ const char* wt_last_error(const wt_ctx* ctx);
 /* Library version, e.g. "libwt 0.1 sm_103a". */
 const char* wt_version(void);
 
+/* Forces of a population state without allocating any memory.  This entry
+ * point has no counterpart in the reference.  It is for callers that cannot
+ * call cudaMalloc: hosts that own every device buffer through their own
+ * allocator or memory budget (or share the lattice through graphics interop
+ * memory) and so cannot create a wt_ctx, and code that must not hit the device
+ * synchronisation cudaMalloc can cause in the middle of a frame.
+ *   f      device, 19*n floats: post-collision populations in the reference's
+ *          order f[i*n + idx] (what wt_read_populations returns)
+ *   solid  device, n u32 flags (0 fluid, 1..3 groups);  emit: device, n floats
+ *          (negative marks a duct cell whose links carry no force), or NULL
+ *   out    host; out->sum / out->raw get the force the next collide-stream step
+ *          takes from this state (as wt_read_force_history / wt_read_forces
+ *          report it), out->steps = 1, the other fields 0.
+ * Scratch is a static device array of WT_NOALLOC_BLOCKS + 1 records (98,400 B)
+ * that every GPU loading the library holds until exit; its address is looked
+ * up on the first call on each device, so make that first call before any
+ * stream capture.  All calls share it: calls that overlap on the GPU race.
+ * Lattices above WT_NOALLOC_MAX_CELLS cells are rejected with
+ * WT_ERR_NOALLOC_LIMIT.  Synchronises `stream` (a cudaStream_t, NULL = legacy
+ * default stream) before returning. */
+#define WT_NOALLOC_BLOCKS 1024u
+#define WT_NOALLOC_MAX_CELLS 134217728ull /* 2^27 */
+#define WT_ERR_NOALLOC_LIMIT (-7)
+int wt_forces_noalloc(const float* f, const uint32_t* solid, const float* emit, uint32_t nx, uint32_t ny,
+                      uint32_t nz, void* stream, wt_forces* out);
+
 #ifdef __cplusplus
 }
 #endif
