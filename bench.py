@@ -189,6 +189,7 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=64, help="LBM steps per kernel-timing launch batch")
+    ap.add_argument("--no-tune", action="store_true", help="skip the block-shape autotuner")
     ap.add_argument("--profile", action="store_true",
                     help="warm-up and timed frames only (for ncu captures); prints a short line")
     args = ap.parse_args()
@@ -225,6 +226,7 @@ def main():
     n = int(dims[0] * dims[1] * dims[2])
     eng = windtunnel.AeroEngine(dims=dims, origin=origin, h=h, sim=sim)
     eng.set_shape_raw(shape)
+    tuned = None if args.no_tune else eng.tune()
     stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
     lbm_per_frame = 8
 
@@ -315,6 +317,8 @@ def main():
                 "workload": desc, "cells": n, "lattice": list(dims), "lbm_steps_per_step": lbm_per_frame,
                 "heat_passes_per_step": 2, "storage": args.storage, "parallelism": f"replicas x{world}",
                 "l2": "working set (populations + cell words) larger than the 126 MB L2; no flush",
+                "block": None if tuned is None else f"{tuned[0]}x{tuned[1]} (autotuned)",
+                "launch": "CUDA graph per frame",
             },
             "roofline": {
                 "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -53,7 +53,36 @@ struct wt_ctx {
   float ks2 = 0.0f;
   float feq_in[19];
   float floor_k[19];
+  float feq_guard[19];
   std::vector<float> tau_host;  // staging copy of tau0_x (pageable: copied before the call returns)
+  bool own_stream = true;
+  unsigned long long* hist_pos = nullptr;  // device: per-step records written so far
+  ReduceArgs* d_reduce = nullptr;          // device: this lattice's reduction record
+  uint32_t bx = 128, by = 1;               // step-kernel block shape
+  uint64_t version = 0;                    // bumped whenever kernel arguments change
+  struct Graph {
+    int n, heat;
+    float dt;
+    uint64_t version;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;               // captured wt_step sequences
+  std::string err;
+};
+
+struct wt_batch {
+  std::vector<wt_ctx*> lat;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  uint32_t storage = 0;
+  uint32_t bx = 128, by = 1;
+  StepArgs* d_args = nullptr;
+  BatchTiles* d_tiles = nullptr;
+  ReduceArgs* d_reduce = nullptr;
+  uint32_t total_blocks = 0;
+  uint32_t pending_cap = 1;
+  uint64_t version = ~0ull;                // sum of member versions the device tables were built for
+  std::vector<wt_ctx::Graph> graphs;
   std::string err;
 };
 
@@ -115,8 +144,32 @@ int apply_sim(wt_ctx* c) {
     const float uu = u * u + 0.0f * 0.0f + 0.0f * 0.0f;
     c->feq_in[i] = Wd(i) * 1.0f * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
     c->floor_k[i] = 6.0f * Wd(i) * (float)CXd(i);
+    // guard reset state (wgsl.ts:239-241): rho = 1, u = uin * 0.5
+    const float gx = u * 0.5f, gy = 0.0f * 0.5f, gz = 0.0f * 0.5f;
+    const float gcu = (float)CXd(i) * gx + (float)CYd(i) * gy + (float)CZd(i) * gz;
+    const float guu = gx * gx + gy * gy + gz * gz;
+    c->feq_guard[i] = Wd(i) * 1.0f * (1.0f + 3.0f * gcu + 4.5f * gcu * gcu - 1.5f * guu);
   }
+  c->version++;
   return WT_OK;
+}
+
+uint32_t warps_per_block(const StepGeom& g);
+
+ReduceArgs reduce_args(const wt_ctx* c) {
+  ReduceArgs r;
+  r.slots = c->slots;
+  r.nslots = c->nslots;
+  r.hist_cap = WT_HIST_CAP;
+  r.hist = c->hist;
+  r.hist_pos = c->hist_pos;
+  r.totals = c->totals;
+  r.raw_totals = c->raw_totals;
+  r.mass_partial = c->mass_partial;
+  r.nmass = c->geom.nblocks * warps_per_block(c->geom);
+  r.mass_out = c->totals + 9;
+  r.counter = c->counters + 1;
+  return r;
 }
 
 // After new flags: cell words, force-carrying blocks and their partial slots.
@@ -159,8 +212,143 @@ int rebuild_links(wt_ctx* c) {
   }
   c->pending_cap = (uint32_t)cap_steps;
   WT_CUDA(c, cudaMemcpyAsync(c->block_slot, map.data(), map.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  ReduceArgs ra = reduce_args(c);
+  WT_CUDA(c, cudaMemcpyAsync(c->d_reduce, &ra, sizeof(ra), cudaMemcpyHostToDevice, c->stream));
   WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->version++;
   return WT_OK;
+}
+
+// Largest float t with sqrt_rn(t) <= 0.35f: sqrt_rn(x) > 0.35f <=> x > t (correctly
+// rounded sqrt is monotonic), so the kernel can test u.u without a square root.
+float guard_threshold() {
+  static float t = [] {
+    float x = 0.35f * 0.35f;
+    while (__builtin_sqrtf(x) > 0.35f) x = __builtin_nextafterf(x, 0.0f);
+    while (__builtin_sqrtf(__builtin_nextafterf(x, 1.0f)) <= 0.35f) x = __builtin_nextafterf(x, 1.0f);
+    return x;
+  }();
+  return t;
+}
+
+uint32_t warps_per_block(const StepGeom& g) { return (g.block.x * g.block.y + 31) / 32; }
+
+StepArgs step_args(const wt_ctx* c) {
+  StepArgs a;
+  a.pop = c->pop; a.cellw = c->cellw; a.solid = c->solid; a.fields = c->fields; a.outlet_u = c->outlet_u;
+  a.tau0_x = c->tau0_x; a.block_slot = c->block_slot; a.mass_partial = c->mass_partial;
+  a.slots = c->slots; a.nslots = c->nslots;
+  a.guard_count = c->counters;
+  a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.n = c->n; a.np = c->np;
+  a.u_in = c->sim.u_in; a.ks2 = c->ks2;
+  memcpy(a.feq_in, c->feq_in, sizeof(a.feq_in));
+  memcpy(a.floor_k, c->floor_k, sizeof(a.floor_k));
+  memcpy(a.feq_guard, c->feq_guard, sizeof(a.feq_guard));
+  a.guard_uu = guard_threshold();
+  return a;
+}
+
+cudaError_t enqueue_heat(wt_ctx* c, int heat_passes, float dt, cudaStream_t s) {
+  HeatArgs h;
+  h.fields = c->fields; h.emit = c->emit;
+  h.nx = c->nx; h.ny = c->ny; h.nz = c->nz;
+  h.dt = dt;
+  h.cool = c->sim.heat_cool; h.diffuse = c->sim.heat_diffuse; h.src_mix = c->sim.heat_src_mix;
+  for (int p = 0; p < heat_passes; p++) {
+    h.tin = (p & 1) ? c->tB : c->tA;
+    h.tout = (p & 1) ? c->tA : c->tB;
+    cudaError_t e = launch_heat(h, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// The kernels of one wt_step call: collide-stream steps (gather/local
+// alternating, fields on the last), a force reduction every pending_cap steps
+// and at the end, then the heat passes.  Pure launches: capturable in a graph.
+cudaError_t enqueue_frame(wt_ctx* c, int n, int heat_passes, float dt, cudaStream_t s) {
+  StepArgs a = step_args(c);
+  uint32_t pending = 0;
+  for (int k = 0; k < n; k++) {
+    const bool last = (k == n - 1);
+    a.slots = c->slots + (size_t)pending * (c->nslots ? c->nslots : 1);
+    cudaError_t e = launch_step(c->sim.storage, (k & 1) == 0, last, c->geom, a, s);
+    if (e != cudaSuccess) return e;
+    pending++;
+    if (pending == c->pending_cap || last) {
+      e = launch_force_reduce(c->d_reduce, 1, pending, last, s);
+      if (e != cudaSuccess) return e;
+      pending = 0;
+    }
+  }
+  return enqueue_heat(c, heat_passes, dt, s);
+}
+
+// Launch a step sequence through a CUDA graph captured once per (n, heat, dt)
+// and argument version; WT_NO_GRAPH=1 launches the kernels directly.
+template <class Owner, class F>
+int run_graphed(Owner* o, std::vector<wt_ctx::Graph>& cache, uint64_t version, int n, int heat, float dt, F&& enqueue) {
+  static const bool no_graph = getenv("WT_NO_GRAPH") && atoi(getenv("WT_NO_GRAPH")) != 0;
+  cudaStream_t s = o->stream;
+  if (no_graph) {
+    cudaError_t e = enqueue(s);
+    if (e != cudaSuccess) { o->err = std::string("kernel launch: ") + cudaGetErrorString(e); return WT_ERR_CUDA; }
+    return WT_OK;
+  }
+  for (size_t i = 0; i < cache.size();) {
+    if (cache[i].version != version) {
+      cudaGraphExecDestroy(cache[i].exec);
+      cache.erase(cache.begin() + i);
+    } else {
+      i++;
+    }
+  }
+  cudaGraphExec_t exec = nullptr;
+  for (auto& g : cache)
+    if (g.n == n && g.heat == heat && g.dt == dt) exec = g.exec;
+  if (!exec) {
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { o->err = std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e); return WT_ERR_CUDA; }
+    cudaError_t le = enqueue(s);
+    e = cudaStreamEndCapture(s, &graph);
+    if (le != cudaSuccess || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      o->err = std::string("graph capture: ") + cudaGetErrorString(le != cudaSuccess ? le : e);
+      return WT_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { o->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e); return WT_ERR_CUDA; }
+    if (cache.size() >= 8) {
+      cudaGraphExecDestroy(cache.front().exec);
+      cache.erase(cache.begin());
+    }
+    cache.push_back({n, heat, dt, version, exec});
+  }
+  cudaError_t e = cudaGraphLaunch(exec, s);
+  if (e != cudaSuccess) { o->err = std::string("cudaGraphLaunch: ") + cudaGetErrorString(e); return WT_ERR_CUDA; }
+  return WT_OK;
+}
+
+// Change the block shape of the step kernels: block maps are rebuilt.
+int set_geometry(wt_ctx* c, uint32_t bx, uint32_t by) {
+  StepGeom g = step_geometry(c->nx, c->ny, c->nz, bx, by);
+  if (g.block.x == c->geom.block.x && g.block.y == c->geom.block.y) return WT_OK;
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  cudaFree(c->block_slot);
+  cudaFree(c->mass_partial);
+  c->device_bytes -= (uint64_t)c->geom.nblocks * 4 + (uint64_t)c->geom.nblocks * warps_per_block(c->geom) * 8;
+  c->block_slot = nullptr;
+  c->mass_partial = nullptr;
+  c->geom = g;
+  c->bx = g.block.x;
+  c->by = g.block.y;
+  int rc;
+  if ((rc = dalloc(c, &c->block_slot, (uint64_t)g.nblocks * 4)) ||
+      (rc = dalloc(c, &c->mass_partial, (uint64_t)g.nblocks * warps_per_block(g) * 8)))
+    return rc;
+  return rebuild_links(c);
 }
 
 int check_ctx(wt_ctx* c) {
@@ -178,7 +366,12 @@ const char* wt_version(void) { return "libwt 0.1 sm_103a"; }
 
 const char* wt_last_error(const wt_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
-int wt_create(const wt_grid* grid, const wt_sim* sim, wt_ctx** out) {
+}  // extern "C"
+
+namespace {
+
+// New lattice; `ext` (may be null) is a stream owned by the caller, e.g. a batch.
+int create_ctx(const wt_grid* grid, const wt_sim* sim, cudaStream_t ext, wt_ctx** out) {
   if (!grid || !sim || !out) return fail(nullptr, WT_ERR_ARG, "wt_create: null argument");
   *out = nullptr;
   if (grid->nx < 8 || grid->ny < 2 || grid->nz < 2) return fail(nullptr, WT_ERR_ARG, "wt_create: grid must be at least 8x2x2");
@@ -204,26 +397,35 @@ int wt_create(const wt_grid* grid, const wt_sim* sim, wt_ctx** out) {
   c->n = n; c->np = np;
   c->elem = sim->storage == WT_STORE_F32 ? 4 : 2;
   c->sm_count = prop.multiProcessorCount;
-  uint32_t bx = 128;
-  if (const char* s = getenv("WT_STEP_BX")) bx = (uint32_t)atoi(s);
-  c->geom = step_geometry(c->nx, c->ny, c->nz, bx);
+  if (const char* s = getenv("WT_STEP_BX")) c->bx = (uint32_t)atoi(s);
+  if (const char* s = getenv("WT_STEP_BY")) c->by = (uint32_t)atoi(s);
+  c->geom = step_geometry(c->nx, c->ny, c->nz, c->bx, c->by);
+  c->bx = c->geom.block.x;
+  c->by = c->geom.block.y;
   int rc = 0;
   auto cleanup = [&](int code) { std::string m = c->err; wt_destroy(c); g_create_error = m; return code; };
-  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-  if (e != cudaSuccess) { c->err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return cleanup(WT_ERR_CUDA); }
+  if (ext) {
+    c->stream = ext;
+    c->own_stream = false;
+  } else {
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { c->err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return cleanup(WT_ERR_CUDA); }
+  }
   if ((rc = dalloc(c, &c->pop, 19 * np * c->elem)) || (rc = dalloc(c, &c->cellw, n * 4)) ||
       (rc = dalloc(c, &c->solid, n)) || (rc = dalloc(c, &c->emit, n * 4)) || (rc = dalloc(c, &c->fields, n * 16)) ||
       (rc = dalloc(c, &c->tA, n * 4)) || (rc = dalloc(c, &c->tB, n * 4)) ||
       (rc = dalloc(c, &c->outlet_u, (uint64_t)c->ny * c->nz * 16)) || (rc = dalloc(c, &c->tau0_x, c->nx * 4)) ||
       (rc = dalloc(c, &c->block_slot, (uint64_t)c->geom.nblocks * 4)) ||
-      (rc = dalloc(c, &c->mass_partial, (uint64_t)c->geom.nblocks * 8)) ||
+      (rc = dalloc(c, &c->mass_partial, (uint64_t)c->geom.nblocks * warps_per_block(c->geom) * 8)) ||
       (rc = dalloc(c, &c->hist, (uint64_t)WT_HIST_CAP * 16 * 8)) || (rc = dalloc(c, &c->totals, 18 * 8)) ||
-      (rc = dalloc(c, &c->raw_totals, 12 * 4)) || (rc = dalloc(c, &c->counters, 4 * 4)))
+      (rc = dalloc(c, &c->raw_totals, 12 * 4)) || (rc = dalloc(c, &c->counters, 4 * 4)) ||
+      (rc = dalloc(c, &c->hist_pos, 8)) || (rc = dalloc(c, &c->d_reduce, sizeof(ReduceArgs))))
     return cleanup(rc);
   if (cudaMemsetAsync(c->solid, 0, n, c->stream) != cudaSuccess || cudaMemsetAsync(c->emit, 0, n * 4, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->totals, 0, 18 * 8, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->raw_totals, 0, 48, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->counters, 0, 16, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->hist_pos, 0, 8, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->pop, 0, 19 * np * c->elem, c->stream) != cudaSuccess) {
     c->err = "initial cudaMemsetAsync failed";
     return cleanup(WT_ERR_CUDA);
@@ -233,15 +435,23 @@ int wt_create(const wt_grid* grid, const wt_sim* sim, wt_ctx** out) {
   return WT_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int wt_create(const wt_grid* grid, const wt_sim* sim, wt_ctx** out) { return create_ctx(grid, sim, nullptr, out); }
+
 int wt_destroy(wt_ctx* c) {
   if (!c) return WT_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
-                  c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters};
+                  c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters,
+                  c->hist_pos, c->d_reduce};
   for (void* p : bufs)
     if (p) cudaFree(p);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
   return WT_OK;
 }
@@ -297,42 +507,13 @@ int wt_step(wt_ctx* c, int n_lbm_steps, int heat_passes, float heat_dt) {
   if (n_lbm_steps < 2 || (n_lbm_steps & 1))
     return fail(c, WT_ERR_ARG, "wt_step: n_lbm_steps must be even and >= 2 (the engine issues max(2, steps - steps % 2))");
   if (heat_passes < 0 || (heat_passes & 1)) return fail(c, WT_ERR_ARG, "wt_step: heat_passes must be 0 or even");
-  StepArgs a;
-  a.pop = c->pop; a.cellw = c->cellw; a.solid = c->solid; a.fields = c->fields; a.outlet_u = c->outlet_u;
-  a.tau0_x = c->tau0_x; a.block_slot = c->block_slot; a.mass_partial = c->mass_partial;
-  a.guard_count = c->counters;
-  a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.n = c->n; a.np = c->np;
-  a.u_in = c->sim.u_in; a.ks2 = c->ks2;
-  memcpy(a.feq_in, c->feq_in, sizeof(a.feq_in));
-  memcpy(a.floor_k, c->floor_k, sizeof(a.floor_k));
-  uint32_t pending = 0;
-  for (int s = 0; s < n_lbm_steps; s++) {
-    const bool last = (s == n_lbm_steps - 1);
-    a.slots = c->slots + (size_t)pending * (c->nslots ? c->nslots : 1);
-    WT_CUDA(c, launch_step(c->sim.storage, (s & 1) == 0, last, c->geom, a, c->stream));
-    pending++;
-    if (pending == c->pending_cap || last) {
-      WT_CUDA(c, launch_force_reduce(c->slots, c->nslots, pending, c->hist, WT_HIST_CAP, c->steps_recorded, c->totals,
-                                     c->raw_totals, c->mass_partial, last ? c->geom.nblocks : 0, c->totals + 9,
-                                     c->counters + 1, c->stream));
-      c->steps_recorded += pending;
-      pending = 0;
-    }
-  }
+  const float dt = heat_dt > 0.0f ? heat_dt : (float)n_lbm_steps / 2.0f;
+  if ((rc = run_graphed(c, c->graphs, c->version, n_lbm_steps, heat_passes, dt,
+                        [&](cudaStream_t s) { return enqueue_frame(c, n_lbm_steps, heat_passes, dt, s); })))
+    return rc;
   c->steps_total += n_lbm_steps;
   c->steps_since_read += n_lbm_steps;
-  if (heat_passes > 0) {
-    HeatArgs h;
-    h.fields = c->fields; h.emit = c->emit;
-    h.nx = c->nx; h.ny = c->ny; h.nz = c->nz;
-    h.dt = heat_dt > 0.0f ? heat_dt : (float)n_lbm_steps / 2.0f;
-    h.cool = c->sim.heat_cool; h.diffuse = c->sim.heat_diffuse; h.src_mix = c->sim.heat_src_mix;
-    for (int p = 0; p < heat_passes; p++) {
-      h.tin = (p & 1) ? c->tB : c->tA;
-      h.tout = (p & 1) ? c->tA : c->tB;
-      WT_CUDA(c, launch_heat(h, c->stream));
-    }
-  }
+  c->steps_recorded += n_lbm_steps;
   return WT_OK;
 }
 
@@ -482,5 +663,301 @@ int wt_sync(wt_ctx* c) {
   WT_CUDA(c, cudaStreamSynchronize(c->stream));
   return WT_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner: time the step kernel under each candidate block shape and keep
+// the fastest.  The lattice state (populations, fields, outlet velocities,
+// force accumulators and history position) is saved before and restored after,
+// so tuning does not advance the simulation.
+// ---------------------------------------------------------------------------
+namespace {
+
+const uint32_t kShapes[][2] = {{128, 1}, {64, 2}, {32, 4}, {256, 1}, {128, 2}, {64, 4}, {32, 8}};
+
+struct Saved {
+  void* pop = nullptr;
+  float4* fields = nullptr;
+  float4* outlet = nullptr;
+  double totals[18];
+  int32_t raw[12];
+  unsigned int counters[4];
+  unsigned long long hist_pos = 0;
+};
+
+int save_state(wt_ctx* c, Saved& sv) {
+  const size_t pb = 19 * c->np * c->elem;
+  WT_CUDA(c, cudaMallocAsync(&sv.pop, pb, c->stream));
+  WT_CUDA(c, cudaMallocAsync((void**)&sv.fields, c->n * 16, c->stream));
+  WT_CUDA(c, cudaMallocAsync((void**)&sv.outlet, (size_t)c->ny * c->nz * 16, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(sv.pop, c->pop, pb, cudaMemcpyDeviceToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(sv.fields, c->fields, c->n * 16, cudaMemcpyDeviceToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(sv.outlet, c->outlet_u, (size_t)c->ny * c->nz * 16, cudaMemcpyDeviceToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(sv.totals, c->totals, sizeof(sv.totals), cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(sv.raw, c->raw_totals, sizeof(sv.raw), cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(sv.counters, c->counters, sizeof(sv.counters), cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(&sv.hist_pos, c->hist_pos, 8, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int restore_state(wt_ctx* c, Saved& sv) {
+  const size_t pb = 19 * c->np * c->elem;
+  WT_CUDA(c, cudaMemcpyAsync(c->pop, sv.pop, pb, cudaMemcpyDeviceToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(c->fields, sv.fields, c->n * 16, cudaMemcpyDeviceToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(c->outlet_u, sv.outlet, (size_t)c->ny * c->nz * 16, cudaMemcpyDeviceToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(c->totals, sv.totals, sizeof(sv.totals), cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(c->raw_totals, sv.raw, sizeof(sv.raw), cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(c->counters, sv.counters, sizeof(sv.counters), cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(c->hist_pos, &sv.hist_pos, 8, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaFreeAsync(sv.pop, c->stream));
+  WT_CUDA(c, cudaFreeAsync(sv.fields, c->stream));
+  WT_CUDA(c, cudaFreeAsync(sv.outlet, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+// ms per LBM step of `step(n)` on stream s (events around `reps` calls of 16 steps)
+template <class Step>
+float time_steps(cudaStream_t s, Step&& step) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  if (step(2) != WT_OK) return -1.0f;  // capture + warm
+  cudaEventRecord(a, s);
+  for (int r = 0; r < 3; r++)
+    if (step(16) != WT_OK) return -1.0f;
+  cudaEventRecord(b, s);
+  cudaEventSynchronize(b);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / 48.0f;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wt_tune(wt_ctx* c, uint32_t* bx_out, uint32_t* by_out, float* ms_out) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  Saved sv;
+  if ((rc = save_state(c, sv))) return rc;
+  const uint64_t steps_total = c->steps_total, since = c->steps_since_read, rec = c->steps_recorded;
+  float best = 1e30f;
+  uint32_t bbx = c->bx, bby = c->by;
+  for (auto& sh : kShapes) {
+    if ((rc = set_geometry(c, sh[0], sh[1]))) return rc;
+    const float ms = time_steps(c->stream, [&](int n) { return wt_step(c, n, 0, 0.0f); });
+    if (ms > 0.0f && ms < best) {
+      best = ms;
+      bbx = c->bx;
+      bby = c->by;
+    }
+  }
+  if ((rc = set_geometry(c, bbx, bby))) return rc;
+  if ((rc = restore_state(c, sv))) return rc;
+  c->steps_total = steps_total;
+  c->steps_since_read = since;
+  c->steps_recorded = rec;
+  if (bx_out) *bx_out = bbx;
+  if (by_out) *by_out = bby;
+  if (ms_out) *ms_out = best;
+  return WT_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many lattices advanced by one kernel launch per step.
+// ---------------------------------------------------------------------------
+namespace {
+
+int bfail(wt_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  else g_create_error = m;
+  return code;
+}
+
+#define WT_BCUDA(b, call)                                                                                 \
+  do {                                                                                                    \
+    cudaError_t e_ = (call);                                                                              \
+    if (e_ != cudaSuccess) return bfail((b), WT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+uint64_t batch_version(const wt_batch* b) {
+  uint64_t v = 0;
+  for (auto* c : b->lat) v = v * 1000003ull + c->version + ((uint64_t)c->bx << 40) + ((uint64_t)c->by << 52);
+  return v;
+}
+
+// Device tables (per-lattice step arguments, block ranges, reduction records).
+int refresh_batch(wt_batch* b) {
+  const uint64_t v = batch_version(b);
+  if (v == b->version) return WT_OK;
+  const size_t count = b->lat.size();
+  std::vector<StepArgs> args(count);
+  std::vector<BatchTiles> tiles(count);
+  std::vector<ReduceArgs> red(count);
+  uint32_t base = 0, cap = WT_PENDING_MAX;
+  for (size_t i = 0; i < count; i++) {
+    wt_ctx* c = b->lat[i];
+    if (c->bx != b->bx || c->by != b->by) {
+      int rc = set_geometry(c, b->bx, b->by);
+      if (rc) return bfail(b, rc, c->err);
+    }
+    args[i] = step_args(c);
+    tiles[i].base = base;
+    tiles[i].gx = c->geom.grid.x;
+    tiles[i].gy = c->geom.grid.y;
+    tiles[i].gz = c->geom.grid.z;
+    base += c->geom.nblocks;
+    red[i] = reduce_args(c);
+    if (c->pending_cap < cap) cap = c->pending_cap;
+  }
+  b->total_blocks = base;
+  b->pending_cap = cap;
+  WT_BCUDA(b, cudaMemcpyAsync(b->d_args, args.data(), count * sizeof(StepArgs), cudaMemcpyHostToDevice, b->stream));
+  WT_BCUDA(b, cudaMemcpyAsync(b->d_tiles, tiles.data(), count * sizeof(BatchTiles), cudaMemcpyHostToDevice, b->stream));
+  WT_BCUDA(b, cudaMemcpyAsync(b->d_reduce, red.data(), count * sizeof(ReduceArgs), cudaMemcpyHostToDevice, b->stream));
+  WT_BCUDA(b, cudaStreamSynchronize(b->stream));
+  b->version = batch_version(b);
+  return WT_OK;
+}
+
+cudaError_t enqueue_batch(wt_batch* b, int n, int heat_passes, float dt, cudaStream_t s) {
+  const uint32_t count = (uint32_t)b->lat.size();
+  const dim3 block(b->bx, b->by, 1);
+  uint32_t pending = 0;
+  for (int k = 0; k < n; k++) {
+    const bool last = (k == n - 1);
+    cudaError_t e = launch_batch_step(b->storage, (k & 1) == 0, last, block, b->total_blocks, b->d_args, b->d_tiles,
+                                      count, pending, s);
+    if (e != cudaSuccess) return e;
+    pending++;
+    if (pending == b->pending_cap || last) {
+      e = launch_force_reduce(b->d_reduce, count, pending, last, s);
+      if (e != cudaSuccess) return e;
+      pending = 0;
+    }
+  }
+  for (auto* c : b->lat) {
+    cudaError_t e = enqueue_heat(c, heat_passes, dt, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wt_batch_create(const wt_grid* grids, uint32_t count, const wt_sim* sim, wt_batch** out) {
+  if (!grids || !sim || !out || count == 0 || count > 1024) return bfail(nullptr, WT_ERR_ARG, "wt_batch_create: bad arguments");
+  *out = nullptr;
+  wt_batch* b = new wt_batch();
+  cudaGetDevice(&b->device);
+  b->storage = sim->storage;
+  auto cleanup = [&](int code) { std::string m = b->err; wt_batch_destroy(b); g_create_error = m; return code; };
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { b->err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return cleanup(WT_ERR_CUDA); }
+  for (uint32_t i = 0; i < count; i++) {
+    wt_ctx* c = nullptr;
+    int rc = create_ctx(&grids[i], sim, b->stream, &c);
+    if (rc) { b->err = "lattice " + std::to_string(i) + ": " + g_create_error; return cleanup(rc); }
+    b->lat.push_back(c);
+  }
+  if (cudaMalloc((void**)&b->d_args, count * sizeof(StepArgs)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_tiles, count * sizeof(BatchTiles)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_reduce, count * sizeof(ReduceArgs)) != cudaSuccess) {
+    b->err = "wt_batch_create: device tables";
+    return cleanup(WT_ERR_NOMEM);
+  }
+  int rc = refresh_batch(b);
+  if (rc) return cleanup(rc);
+  *out = b;
+  return WT_OK;
+}
+
+int wt_batch_destroy(wt_batch* b) {
+  if (!b) return WT_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto* c : b->lat) wt_destroy(c);
+  if (b->d_args) cudaFree(b->d_args);
+  if (b->d_tiles) cudaFree(b->d_tiles);
+  if (b->d_reduce) cudaFree(b->d_reduce);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return WT_OK;
+}
+
+uint32_t wt_batch_count(const wt_batch* b) { return b ? (uint32_t)b->lat.size() : 0u; }
+
+wt_ctx* wt_batch_lattice(wt_batch* b, uint32_t i) { return (b && i < b->lat.size()) ? b->lat[i] : nullptr; }
+
+int wt_batch_step(wt_batch* b, int n_lbm_steps, int heat_passes, float heat_dt) {
+  if (!b) return WT_ERR_ARG;
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, WT_ERR_CUDA, "cudaSetDevice");
+  if (n_lbm_steps < 2 || (n_lbm_steps & 1)) return bfail(b, WT_ERR_ARG, "wt_batch_step: n_lbm_steps must be even and >= 2");
+  if (heat_passes < 0 || (heat_passes & 1)) return bfail(b, WT_ERR_ARG, "wt_batch_step: heat_passes must be 0 or even");
+  int rc = refresh_batch(b);
+  if (rc) return rc;
+  const float dt = heat_dt > 0.0f ? heat_dt : (float)n_lbm_steps / 2.0f;
+  if ((rc = run_graphed(b, b->graphs, b->version, n_lbm_steps, heat_passes, dt,
+                        [&](cudaStream_t s) { return enqueue_batch(b, n_lbm_steps, heat_passes, dt, s); })))
+    return rc;
+  for (auto* c : b->lat) {
+    c->steps_total += n_lbm_steps;
+    c->steps_since_read += n_lbm_steps;
+    c->steps_recorded += n_lbm_steps;
+  }
+  return WT_OK;
+}
+
+int wt_batch_tune(wt_batch* b, uint32_t* bx_out, uint32_t* by_out, float* ms_out) {
+  if (!b) return WT_ERR_ARG;
+  std::vector<Saved> sv(b->lat.size());
+  std::vector<uint64_t> keep(3 * b->lat.size());
+  for (size_t i = 0; i < b->lat.size(); i++) {
+    wt_ctx* c = b->lat[i];
+    int rc = save_state(c, sv[i]);
+    if (rc) return bfail(b, rc, c->err);
+    keep[3 * i] = c->steps_total; keep[3 * i + 1] = c->steps_since_read; keep[3 * i + 2] = c->steps_recorded;
+  }
+  float best = 1e30f;
+  uint32_t bbx = b->bx, bby = b->by;
+  for (auto& sh : kShapes) {
+    b->bx = sh[0];
+    b->by = sh[1];
+    const float ms = time_steps(b->stream, [&](int n) { return wt_batch_step(b, n, 0, 0.0f); });
+    if (ms > 0.0f && ms < best) {
+      best = ms;
+      bbx = b->bx;
+      bby = b->by;
+    }
+  }
+  b->bx = bbx;
+  b->by = bby;
+  int rc = refresh_batch(b);
+  if (rc) return rc;
+  for (size_t i = 0; i < b->lat.size(); i++) {
+    wt_ctx* c = b->lat[i];
+    if ((rc = restore_state(c, sv[i]))) return bfail(b, rc, c->err);
+    c->steps_total = keep[3 * i]; c->steps_since_read = keep[3 * i + 1]; c->steps_recorded = keep[3 * i + 2];
+  }
+  if (bx_out) *bx_out = bbx;
+  if (by_out) *by_out = bby;
+  if (ms_out) *ms_out = best;
+  return WT_OK;
+}
+
+void* wt_batch_stream(wt_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+const char* wt_batch_last_error(const wt_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
 
 }  // extern "C"

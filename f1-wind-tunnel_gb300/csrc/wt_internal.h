@@ -16,7 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
-#include "../../include/wt.h"
+#include "wt.h"
 
 #define WT_HIST_CAP 16384u    // per-step force records kept on the device (ring)
 #define WT_PENDING_MAX 64u    // steps whose partials wait for one reduction launch
@@ -39,13 +39,16 @@ struct StepArgs {
   const float* tau0_x;
   const int32_t* block_slot;   // block -> slot or -1
   ForceSlot* slots;            // this step's partial records [nslots]
-  double* mass_partial;        // [nblocks] (field steps only)
+  uint32_t nslots;             // records per step (force-carrying blocks)
+  double* mass_partial;        // [nblocks * warps per block] (field steps only)
   unsigned int* guard_count;
   uint32_t nx, ny, nz;
   uint64_t n, np;
   float u_in, ks2;             // ks2 = (18*1.41421356 as f32) * smag * smag
+  float guard_uu;              // largest u.u whose square root rounds to <= 0.35f
   float feq_in[19];            // feq(i, 1, (u_in, 0, 0))
   float floor_k[19];           // 6 * w_i * c_ix (belt term coefficient)
+  float feq_guard[19];         // feq(i, 1, (u_in/2, 0, 0)): the divergence guard's reset state
 };
 
 struct HeatArgs {
@@ -63,16 +66,37 @@ struct StepGeom {
   uint32_t nblocks;
 };
 
-StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx);
+StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx, uint32_t by);
+
+// Block ranges of the lattices of a batch launch (see batch_step_kernel).
+struct BatchTiles {
+  uint32_t base;        // first block of this lattice
+  uint32_t gx, gy, gz;  // the lattice's grid in blocks
+};
 
 // wt_lbm.cu
 cudaError_t launch_init(uint32_t storage, void* pop, float4* fields, float4* outlet_u, uint32_t nx, uint32_t ny,
                         uint32_t nz, uint64_t np, float u_in, cudaStream_t s);
 cudaError_t launch_step(uint32_t storage, bool gather, bool write_fields, const StepGeom& g, const StepArgs& a,
                         cudaStream_t s);
-cudaError_t launch_force_reduce(const ForceSlot* slots, uint32_t nslots, uint32_t nsteps, double* hist,
-                                uint32_t hist_cap, uint64_t hist_base, double* totals, int32_t* raw_totals,
-                                const double* mass_partial, uint32_t nmass, double* mass_out, unsigned int* counter,
+cudaError_t launch_batch_step(uint32_t storage, bool gather, bool write_fields, dim3 block, uint32_t total_blocks,
+                              const StepArgs* args, const BatchTiles* tiles, uint32_t count, uint32_t pending,
+                              cudaStream_t s);
+// Per-lattice arguments of the force reduction (one record per lattice, in device memory).
+struct ReduceArgs {
+  const ForceSlot* slots;
+  uint32_t nslots;
+  uint32_t hist_cap;
+  double* hist;
+  unsigned long long* hist_pos;  // steps recorded so far (advanced by the reduction itself)
+  double* totals;
+  int32_t* raw_totals;
+  const double* mass_partial;
+  uint32_t nmass;
+  double* mass_out;
+  unsigned int* counter;
+};
+cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t nsteps, bool with_mass,
                                 cudaStream_t s);
 cudaError_t launch_read_pop(uint32_t storage, const void* pop, float* out, uint32_t n, uint64_t np, cudaStream_t s);
 cudaError_t launch_write_pop(uint32_t storage, const float* in, void* pop, uint32_t n, uint64_t np, cudaStream_t s);

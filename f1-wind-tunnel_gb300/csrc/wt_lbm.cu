@@ -75,7 +75,7 @@ __device__ __forceinline__ bool is_bad(float x) { return (__float_as_uint(x) & 0
 // Moments, divergence guard, duct relaxation, regularized + Smagorinsky collision
 // (wgsl.ts:231-272).  f[] in, fo[] out.
 __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19], float tau0, float u_in, float ks2,
-                                           bool duct) {
+                                           bool duct, const float (&feq_guard)[19], float guard_uu) {
   CellOut o;
   float rho = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f;
   sfor<19>([&](auto I) {
@@ -91,20 +91,17 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
   const float den = (rho < 1e-4f) ? 1e-4f : rho;
   float ux = mx / den, uy = my / den, uz = mz / den;
   float g[19];
+  // length(u) > 0.35 (wgsl.ts:238) <=> u.u > guard_uu: sqrt is correctly rounded and
+  // monotonic, and guard_uu is the largest float whose square root rounds to <= 0.35f.
   bool guard = is_bad(rho) || is_bad(ux) || is_bad(uy) || is_bad(uz) || rho < 0.3f || rho > 3.0f ||
-               __fsqrt_rn(ux * ux + uy * uy + uz * uz) > 0.35f;
+               (ux * ux + uy * uy + uz * uz) > guard_uu;
+  // Divergence guard (wgsl.ts:238-243): rho = 1, u = u_in/2, f = feq(1, u); the
+  // equilibria are the same for every cell and come precomputed from the host.
   if (guard) {
     rho = 1.0f;
     ux = u_in * 0.5f; uy = 0.0f; uz = 0.0f;
-    const float uu = ux * ux + uy * uy + uz * uz;
-    sfor<19>([&](auto I) {
-      constexpr int i = I;
-      const float cu = cdot<i>(ux, uy, uz);
-      g[i] = Wd(i) * rho * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
-    });
-  } else {
-    sfor<19>([&](auto I) { g[I] = f[I]; });
   }
+  sfor<19>([&](auto I) { g[I] = guard ? feq_guard[I] : f[I]; });
   if (duct) {
     const float t = 0.04f, tu = 1.0f - 0.04f;
     ux = ux * tu + (0.55f * u_in) * t;
@@ -115,13 +112,21 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
   const float uu15 = 1.5f * uu;
   const float wr0 = Wd(0) * rho, wr1 = Wd(1) * rho, wr2 = Wd(7) * rho;
   float eq[19];
+  // Opposite directions share 3 c.u (exact negation) and 4.5 (c.u)^2 (identical bits).
+  eq[0] = wr0 * (1.0f + 3.0f * 0.0f + 4.5f * 0.0f * 0.0f - uu15);
+  sfor<9>([&](auto P) {
+    constexpr int i = 2 * P + 1;  // odd member of the pair (i, i + 1)
+    const float cu = cdot<i>(ux, uy, uz);
+    const float t3 = 3.0f * cu;
+    const float t45 = 4.5f * cu * cu;
+    const float wr = (i < 7 ? wr1 : wr2);
+    eq[i] = wr * (1.0f + t3 + t45 - uu15);
+    eq[i + 1] = wr * (1.0f - t3 + t45 - uu15);
+  });
   float pxx = 0.0f, pyy = 0.0f, pzz = 0.0f, pxy = 0.0f, pxz = 0.0f, pyz = 0.0f;
   sfor<19>([&](auto I) {
     constexpr int i = I;
     constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
-    const float cu = cdot<i>(ux, uy, uz);
-    const float wr = (i == 0) ? wr0 : (i < 7 ? wr1 : wr2);
-    eq[i] = wr * (1.0f + 3.0f * cu + 4.5f * cu * cu - uu15);
     const float ne = g[i] - eq[i];
     if constexpr (cx != 0) pxx = pxx + ne;
     if constexpr (cy != 0) pyy = pyy + ne;
@@ -135,7 +140,7 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
   });
   const float q = __fsqrt_rn(pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
   const float tau = 0.5f * (tau0 + __fsqrt_rn(tau0 * tau0 + __fdiv_rn(ks2 * q, rho)));
-  const float omega = __fdiv_rn(1.0f, tau);
+  const float omega = __frcp_rn(tau);  // correctly rounded 1/tau, the same bits as 1.0f / tau
   const float c1 = (1.0f - omega) * 4.5f;
   const float k0 = c1 * Wd(0), k1 = c1 * Wd(1), k2 = c1 * Wd(7);
   // (c_a c_a - 1/3) with the reference's f32 third: 1 - third rounds to 0x1.555554p-1
@@ -144,8 +149,9 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
   const float a_yy = (1.0f - third) * pyy, b_yy = (0.0f - third) * pyy;
   const float a_zz = (1.0f - third) * pzz, b_zz = (0.0f - third) * pzz;
   const float pxy2 = 2.0f * pxy, pxz2 = 2.0f * pxz, pyz2 = 2.0f * pyz;
-  sfor<19>([&](auto I) {
-    constexpr int i = I;
+  fo[0] = eq[0] + k0 * ((b_xx + b_yy) + b_zz);
+  sfor<9>([&](auto P) {  // (c_a c_b - delta/3) is the same for i and opp(i)
+    constexpr int i = 2 * P + 1;
     constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
     float qp = ((cx != 0) ? a_xx : b_xx) + ((cy != 0) ? a_yy : b_yy);
     qp = qp + ((cz != 0) ? a_zz : b_zz);
@@ -155,8 +161,9 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
     if constexpr (cx * cz < 0) qp = qp - pxz2;
     if constexpr (cy * cz > 0) qp = qp + pyz2;
     if constexpr (cy * cz < 0) qp = qp - pyz2;
-    const float kw = (i == 0) ? k0 : (i < 7 ? k1 : k2);
-    fo[i] = eq[i] + kw * qp;
+    const float kq = (i < 7 ? k1 : k2) * qp;
+    fo[i] = eq[i] + kq;
+    fo[i + 1] = eq[i + 1] + kq;
   });
   o.ux = ux; o.uy = uy; o.uz = uz; o.rho = rho; o.guard = guard;
   return o;
@@ -189,13 +196,27 @@ __device__ __forceinline__ void link_force(float v, uint32_t group, float (&gf)[
   }
 }
 
+// ---------------------------------------------------------------------------
+// One thread per cell, blocks of 128 cells along x (grid nx/128 x ny x nz).
+// All 19 population reads are issued before the collision.  Warps away from
+// the lattice faces take a short path: in the gather step each direction reads
+// either the neighbour's slot or, for a bounce-back link, the cell's own slot
+// (one select, one load); faces take the full boundary precedence.
+// (A TMA-staged persistent variant - 19 cp.async.bulk row windows per tile into
+// a double-buffered shared-memory stage - was measured slower on this kernel:
+// 19.9 vs 26 GLUPS on the 256x96x80 F1, so it is not used.)
+// ---------------------------------------------------------------------------
+constexpr uint32_t TILE = 128;
+
+// One block's cells of one lattice.  bid/gdim are the block coordinates and grid
+// of that lattice's tiling; slots is where this step's force records go.
 template <class St, bool GATHER, bool FIELDS>
-__global__ void __launch_bounds__(128) step_kernel(StepArgs a) {
+__device__ __forceinline__ void step_tile(const StepArgs& a, ForceSlot* slots, uint3 bid, uint3 gdim) {
   const uint8_t* __restrict__ solid_u8 = a.solid;
   const uint32_t nx = a.nx, ny = a.ny, nz = a.nz;
-  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
-  const uint32_t z = blockIdx.z;
+  const uint32_t x = bid.x * blockDim.x + threadIdx.x;
+  const uint32_t y = bid.y * blockDim.y + threadIdx.y;
+  const uint32_t z = bid.z;
   const bool in = (x < nx) && (y < ny);
   const uint32_t nxy = nx * ny;
   const uint32_t np = (uint32_t)a.np;
@@ -285,7 +306,7 @@ __global__ void __launch_bounds__(128) step_kernel(StepArgs a) {
     }
 
     // ---------------------------------------------------------------- collide
-    const CellOut o = collide(f, fo, __ldg(a.tau0_x + x), a.u_in, a.ks2, (cw & CW_DUCT) != 0);
+    const CellOut o = collide(f, fo, __ldg(a.tau0_x + x), a.u_in, a.ks2, (cw & CW_DUCT) != 0, a.feq_guard, a.guard_uu);
     if (o.guard) {
 #pragma unroll
       for (int k = 0; k < 9; k++) gf[k] = 0.0f;
@@ -346,19 +367,24 @@ __global__ void __launch_bounds__(128) step_kernel(StepArgs a) {
   // -------------------------------------------------------------- reductions
   const uint32_t lane = threadIdx.x & 31u, warp = (threadIdx.x + blockDim.x * threadIdx.y) >> 5;
   const uint32_t nwarps = (blockDim.x * blockDim.y + 31) >> 5;
-  const uint32_t blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  const uint32_t blk = bid.x + gdim.x * (bid.y + gdim.y * bid.z);
   const unsigned gb = __ballot_sync(0xffffffffu, guard);
   if (gb && lane == 0) atomicAdd(a.guard_count, (unsigned)__popc(gb));
-
+  if constexpr (FIELDS) {  // per-warp FP64 mass partial, reduced in a fixed order later
+    double m = (in && !(cw & CW_SOLID)) ? (double)rho_cell : 0.0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) m += __shfl_down_sync(0xffffffffu, m, s);
+    if (lane == 0) a.mass_partial[(size_t)blk * nwarps + warp] = m;
+  }
+  const int32_t slot = __ldg(a.block_slot + blk);
+  if (slot < 0) return;  // no force-carrying link in this block: no barrier, no record
   __shared__ double s_f[9][8];
   __shared__ int32_t s_r[6][8];
-  __shared__ double s_m[8];
-  const int32_t slot = __ldg(a.block_slot + blk);
-  if (slot >= 0) {
+  {
     double d[9];
     int32_t r[6];
 #pragma unroll
-    for (int k = 0; k < 9; k++) d[k] = (double)gf[k];
+    for (int q = 0; q < 9; q++) d[q] = (double)gf[q];
 #pragma unroll
     for (int g = 0; g < 3; g++) {
       r[2 * g] = (gf[3 * g] != 0.0f) ? __float2int_rn(gf[3 * g] * 10000.0f) : 0;
@@ -367,44 +393,57 @@ __global__ void __launch_bounds__(128) step_kernel(StepArgs a) {
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) {
 #pragma unroll
-      for (int k = 0; k < 9; k++) d[k] += __shfl_down_sync(0xffffffffu, d[k], s);
+      for (int q = 0; q < 9; q++) d[q] += __shfl_down_sync(0xffffffffu, d[q], s);
 #pragma unroll
-      for (int k = 0; k < 6; k++) r[k] = (int32_t)((uint32_t)r[k] + (uint32_t)__shfl_down_sync(0xffffffffu, r[k], s));
+      for (int q = 0; q < 6; q++) r[q] = (int32_t)((uint32_t)r[q] + (uint32_t)__shfl_down_sync(0xffffffffu, r[q], s));
     }
     if (lane == 0) {
 #pragma unroll
-      for (int k = 0; k < 9; k++) s_f[k][warp] = d[k];
+      for (int q = 0; q < 9; q++) s_f[q][warp] = d[q];
 #pragma unroll
-      for (int k = 0; k < 6; k++) s_r[k][warp] = r[k];
+      for (int q = 0; q < 6; q++) s_r[q][warp] = r[q];
     }
-  }
-  if constexpr (FIELDS) {
-    double m = (in && !(cw & CW_SOLID)) ? (double)rho_cell : 0.0;
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) m += __shfl_down_sync(0xffffffffu, m, s);
-    if (lane == 0) s_m[warp] = m;
   }
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    if (slot >= 0) {
-      ForceSlot& out = a.slots[slot];
-      for (int k = 0; k < 9; k++) {
-        double t = 0.0;
-        for (uint32_t w = 0; w < nwarps; w++) t += s_f[k][w];
-        out.f[k] = t;
-      }
-      for (int k = 0; k < 6; k++) {
-        uint32_t t = 0;
-        for (uint32_t w = 0; w < nwarps; w++) t += (uint32_t)s_r[k][w];
-        out.raw[k] = (int32_t)t;
-      }
+    ForceSlot& out = slots[slot];
+    for (int q = 0; q < 9; q++) {
+      double tt = 0.0;
+      for (uint32_t w = 0; w < nwarps; w++) tt += s_f[q][w];
+      out.f[q] = tt;
     }
-    if constexpr (FIELDS) {
-      double t = 0.0;
-      for (uint32_t w = 0; w < nwarps; w++) t += s_m[w];
-      a.mass_partial[blk] = t;
+    for (int q = 0; q < 6; q++) {
+      uint32_t tt = 0;
+      for (uint32_t w = 0; w < nwarps; w++) tt += (uint32_t)s_r[q][w];
+      out.raw[q] = (int32_t)tt;
     }
   }
+}
+
+template <class St, bool GATHER, bool FIELDS>
+__global__ void __launch_bounds__(256, 4) step_kernel(StepArgs a) {
+  step_tile<St, GATHER, FIELDS>(a, a.slots, blockIdx, make_uint3(gridDim.x, gridDim.y, gridDim.z));
+}
+
+// Many lattices in one launch: block b belongs to the lattice L with
+// tile_base[L] <= b < tile_base[L+1]; its coordinates follow that lattice's grid.
+template <class St, bool GATHER, bool FIELDS>
+__global__ void __launch_bounds__(256, 4) batch_step_kernel(const StepArgs* __restrict__ args,
+                                                            const BatchTiles* __restrict__ tiles, uint32_t count,
+                                                            uint32_t pending) {
+  const uint32_t b = blockIdx.x;
+  uint32_t lo = 0, hi = count;  // binary search: largest L with base[L] <= b
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&tiles[mid].base) <= b) lo = mid;
+    else hi = mid;
+  }
+  const BatchTiles tl = tiles[lo];
+  const uint32_t t = b - tl.base;
+  const uint3 gdim = make_uint3(tl.gx, tl.gy, tl.gz);
+  const uint3 bid = make_uint3(t % tl.gx, (t / tl.gx) % tl.gy, t / (tl.gx * tl.gy));
+  const StepArgs& a = args[lo];
+  step_tile<St, GATHER, FIELDS>(a, a.slots + (size_t)pending * a.nslots, bid, gdim);
 }
 
 // Canonical initial state (LBM_INIT, wgsl.ts:147-155): f*_j = feq_j(1, (u_in,0,0))
@@ -477,63 +516,86 @@ __global__ void resample_kernel(const float4* coarse, uint32_t cx, uint32_t cy, 
   if (x == nx - 1) outlet_u[y + ny * z] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
 
-// Deterministic reduction of the pending steps' partial records: one block per
-// step sums its slots in a fixed order and writes the step's record to the
-// history ring; the last block to finish folds the steps into the running
-// totals in step order.
-__global__ void force_reduce_kernel(const ForceSlot* slots, uint32_t nslots, uint32_t nsteps, double* hist,
-                                    uint32_t hist_cap, uint64_t hist_base, double* totals, int32_t* raw_totals,
-                                    const double* mass_partial, uint32_t nmass, double* mass_out,
-                                    unsigned int* counter) {
-  const uint32_t step = blockIdx.x;
-  const uint32_t t = threadIdx.x;
-  __shared__ double sd[256];
-  __shared__ uint32_t sr[256];
+// Deterministic reduction of the pending steps' partial records: block s < nsteps
+// sums step s's records (each thread a fixed strided subset with all 15
+// components in registers, then a fixed shuffle tree and the warps in order)
+// into the history ring; block nsteps sums the mass partials; the last block to
+// finish folds the steps into the running totals in step order.
+constexpr uint32_t RED_THREADS = 256;
+
+__device__ __forceinline__ double block_sum_d(double v, double* sm) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+  if (lane == 0) sm[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (uint32_t w = 0; w < RED_THREADS / 32; w++) t += sm[w];
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceArgs* __restrict__ all, uint32_t nsteps,
+                                                                   uint32_t with_mass) {
+  __shared__ double sm[RED_THREADS / 32];
+  __shared__ uint32_t smr[6][RED_THREADS / 32];
   __shared__ bool last;
-  const ForceSlot* base = slots + (size_t)step * nslots;
-  double* rec = hist + ((hist_base + step) % hist_cap) * 16;
-  for (int k = 0; k < 15; k++) {
+  const ReduceArgs& ra = all[blockIdx.y];
+  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  const uint64_t hist_base = *ra.hist_pos;
+  if (blockIdx.x < nsteps) {
+    const uint32_t step = blockIdx.x;
+    const ForceSlot* base = ra.slots + (size_t)step * ra.nslots;
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t racc[6] = {0, 0, 0, 0, 0, 0};
+    for (uint32_t s = t; s < ra.nslots; s += RED_THREADS) {
+      const ForceSlot r = base[s];
+#pragma unroll
+      for (int k = 0; k < 9; k++) acc[k] += r.f[k];
+#pragma unroll
+      for (int k = 0; k < 6; k++) racc[k] += (uint32_t)r.raw[k];
+    }
+    double* rec = ra.hist + ((hist_base + step) % ra.hist_cap) * 16;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      const double v = block_sum_d(acc[k], sm);
+      if (t == 0) rec[k] = v;
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1)
+#pragma unroll
+      for (int k = 0; k < 6; k++) racc[k] += __shfl_down_sync(0xffffffffu, racc[k], s);
+    if (lane == 0)
+      for (int k = 0; k < 6; k++) smr[k][warp] = racc[k];
+    __syncthreads();
+    if (t == 0)
+      for (int k = 0; k < 6; k++) {
+        uint32_t v = 0;
+        for (uint32_t w = 0; w < RED_THREADS / 32; w++) v += smr[k][w];
+        rec[9 + k] = (double)(int32_t)v;
+      }
+  } else if (with_mass) {
     double acc = 0.0;
-    uint32_t racc = 0;
-    for (uint32_t s = t; s < nslots; s += blockDim.x) {
-      if (k < 9) acc += base[s].f[k];
-      else racc += (uint32_t)base[s].raw[k - 9];
-    }
-    sd[t] = acc;
-    sr[t] = racc;
-    __syncthreads();
-    for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (t < w) { sd[t] += sd[t + w]; sr[t] += sr[t + w]; }
-      __syncthreads();
-    }
-    if (t == 0) rec[k] = (k < 9) ? sd[0] : (double)(int32_t)sr[0];
-    __syncthreads();
-  }
-  if (step == nsteps - 1 && nmass > 0) {
-    double acc = 0.0;
-    for (uint32_t s = t; s < nmass; s += blockDim.x) acc += mass_partial[s];
-    sd[t] = acc;
-    __syncthreads();
-    for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (t < w) sd[t] += sd[t + w];
-      __syncthreads();
-    }
-    if (t == 0) *mass_out = sd[0];
+    for (uint32_t s = t; s < ra.nmass; s += RED_THREADS) acc += ra.mass_partial[s];
+    const double v = block_sum_d(acc, sm);
+    if (t == 0) *ra.mass_out = v;
   }
   __threadfence();
-  if (t == 0) last = (atomicAdd(counter, 1u) == nsteps - 1);
+  if (t == 0) last = (atomicAdd(ra.counter, 1u) == gridDim.x - 1);
   __syncthreads();
   if (last && t == 0) {
     __threadfence();
     for (uint32_t s = 0; s < nsteps; s++) {
-      const double* r = hist + ((hist_base + s) % hist_cap) * 16;
-      for (int k = 0; k < 9; k++) totals[k] += r[k];
+      const double* r = ra.hist + ((hist_base + s) % ra.hist_cap) * 16;
+      for (int k = 0; k < 9; k++) ra.totals[k] += r[k];
       for (int g = 0; g < 3; g++) {
-        raw_totals[3 * g] = (int32_t)((uint32_t)raw_totals[3 * g] + (uint32_t)(int32_t)r[9 + 2 * g]);
-        raw_totals[3 * g + 1] = (int32_t)((uint32_t)raw_totals[3 * g + 1] + (uint32_t)(int32_t)r[10 + 2 * g]);
+        ra.raw_totals[3 * g] = (int32_t)((uint32_t)ra.raw_totals[3 * g] + (uint32_t)(int32_t)r[9 + 2 * g]);
+        ra.raw_totals[3 * g + 1] = (int32_t)((uint32_t)ra.raw_totals[3 * g + 1] + (uint32_t)(int32_t)r[10 + 2 * g]);
       }
     }
-    *counter = 0u;
+    *ra.hist_pos = hist_base + nsteps;
+    *ra.counter = 0u;
   }
 }
 
@@ -545,6 +607,19 @@ cudaError_t launch_step_t(bool gather, bool fields, const StepGeom& g, const Ste
   } else {
     if (fields) step_kernel<St, false, true><<<g.grid, g.block, 0, s>>>(a);
     else step_kernel<St, false, false><<<g.grid, g.block, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+template <class St>
+cudaError_t launch_batch_t(bool gather, bool fields, dim3 block, uint32_t total_blocks, const StepArgs* args,
+                           const BatchTiles* tiles, uint32_t count, uint32_t pending, cudaStream_t s) {
+  if (gather) {
+    if (fields) batch_step_kernel<St, true, true><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
+    else batch_step_kernel<St, true, false><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
+  } else {
+    if (fields) batch_step_kernel<St, false, true><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
+    else batch_step_kernel<St, false, false><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
   }
   return cudaGetLastError();
 }
@@ -574,11 +649,12 @@ cudaError_t by_storage(uint32_t storage, F&& f) {
 
 }  // namespace
 
-StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx) {
+// Block shape (bx cells along x) x (by rows along y); bx a multiple of 32 and
+// bx * by <= 256 (the kernels' launch bounds).  The autotuner picks the shape.
+StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx, uint32_t by) {
+  if (bx == 0 || bx % 32 != 0 || bx > 256) bx = TILE;
+  if (by == 0 || bx * by > 256) by = 1;
   StepGeom g;
-  if (bx == 0 || bx > BX_MAX) bx = 128;
-  uint32_t by = 128 / bx;
-  if (by == 0) by = 1;
   g.block = dim3(bx, by, 1);
   g.grid = dim3((nx + bx - 1) / bx, (ny + by - 1) / by, nz);
   g.nblocks = g.grid.x * g.grid.y * g.grid.z;
@@ -603,13 +679,18 @@ cudaError_t launch_step(uint32_t storage, bool gather, bool write_fields, const 
   return by_storage(storage, [&](auto st) { return launch_step_t<decltype(st)>(gather, write_fields, g, a, s); });
 }
 
-cudaError_t launch_force_reduce(const ForceSlot* slots, uint32_t nslots, uint32_t nsteps, double* hist,
-                                uint32_t hist_cap, uint64_t hist_base, double* totals, int32_t* raw_totals,
-                                const double* mass_partial, uint32_t nmass, double* mass_out, unsigned int* counter,
+cudaError_t launch_batch_step(uint32_t storage, bool gather, bool write_fields, dim3 block, uint32_t total_blocks,
+                              const StepArgs* args, const BatchTiles* tiles, uint32_t count, uint32_t pending,
+                              cudaStream_t s) {
+  return by_storage(storage, [&](auto st) {
+    return launch_batch_t<decltype(st)>(gather, write_fields, block, total_blocks, args, tiles, count, pending, s);
+  });
+}
+
+cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t nsteps, bool with_mass,
                                 cudaStream_t s) {
-  if (nsteps == 0) return cudaSuccess;
-  force_reduce_kernel<<<nsteps, 256, 0, s>>>(slots, nslots, nsteps, hist, hist_cap, hist_base, totals, raw_totals,
-                                             mass_partial, nmass, mass_out, counter);
+  if (nsteps == 0 || count == 0) return cudaSuccess;
+  force_reduce_kernel<<<dim3(nsteps + 1, count), RED_THREADS, 0, s>>>(args, nsteps, with_mass ? 1u : 0u);
   return cudaGetLastError();
 }
 

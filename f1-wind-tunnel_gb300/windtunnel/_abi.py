@@ -90,6 +90,15 @@ _PROTOS = {
     "wt_stream": (_vp, [_vp]),
     "wt_sync": (ctypes.c_int, [_vp]),
     "wt_last_error": (ctypes.c_char_p, [_vp]),
+    "wt_tune": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "wt_batch_create": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.POINTER(Sim), ctypes.POINTER(_vp)]),
+    "wt_batch_destroy": (ctypes.c_int, [_vp]),
+    "wt_batch_count": (ctypes.c_uint32, [_vp]),
+    "wt_batch_lattice": (_vp, [_vp, ctypes.c_uint32]),
+    "wt_batch_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+    "wt_batch_tune": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "wt_batch_stream": (_vp, [_vp]),
+    "wt_batch_last_error": (ctypes.c_char_p, [_vp]),
     "wt_version": (ctypes.c_char_p, []),
 }
 

@@ -152,7 +152,7 @@ class ForceReading:
 
 
 class AeroEngine:
-    def __init__(self, quality="medium", dims=None, h=None, origin=None, sim=None, lib=None):
+    def __init__(self, quality="medium", dims=None, h=None, origin=None, sim=None, lib=None, _ctx=None):
         nx, ny, nz = dims if dims is not None else QUALITIES[quality]
         self.dims = (int(nx), int(ny), int(nz))
         self.n = nx * ny * nz
@@ -167,18 +167,23 @@ class AeroEngine:
             g.origin[k] = self.origin[k]
         g.h = self.h
         self._grid = g
-        ctx = ctypes.c_void_p()
-        rc = self.lib.wt_create(ctypes.byref(g), ctypes.byref(self.sim), ctypes.byref(ctx))
-        if rc != _abi.WT_OK:
-            raise _abi.WindTunnelError(rc, "wt_create: " + self.lib.wt_last_error(None).decode())
-        self.ctx = ctx
+        self._owned = _ctx is None
+        if _ctx is not None:  # a lattice that belongs to a batch
+            self.ctx = ctypes.c_void_p(_ctx)
+        else:
+            ctx = ctypes.c_void_p()
+            rc = self.lib.wt_create(ctypes.byref(g), ctypes.byref(self.sim), ctypes.byref(ctx))
+            if rc != _abi.WT_OK:
+                raise _abi.WindTunnelError(rc, "wt_create: " + self.lib.wt_last_error(None).decode())
+            self.ctx = ctx
         self.shape_params = None
         self.steps_since_read = 0
 
     # -- lifetime ---------------------------------------------------------------
     def close(self):
         if getattr(self, "ctx", None):
-            self.lib.wt_destroy(self.ctx)
+            if getattr(self, "_owned", True):
+                self.lib.wt_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):
@@ -300,6 +305,12 @@ class AeroEngine:
         assert four == 4
         self._check(self.lib.wt_reset_from(self.ctx, c.ctypes.data, cx, cy, cz), "wt_reset_from")
 
+    def tune(self):
+        """Autotune the collide-stream block shape (state is preserved); returns (bx, by, ms/step)."""
+        bx, by, ms = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_float()
+        self._check(self.lib.wt_tune(self.ctx, ctypes.byref(bx), ctypes.byref(by), ctypes.byref(ms)), "wt_tune")
+        return bx.value, by.value, ms.value
+
     def info(self):
         i = _abi.Info()
         self._check(self.lib.wt_info_get(self.ctx, ctypes.byref(i)), "wt_info_get")
@@ -310,3 +321,60 @@ class AeroEngine:
 
     def sync(self):
         self._check(self.lib.wt_sync(self.ctx), "wt_sync")
+
+
+class AeroBatch:
+    """Many lattices advanced together by one kernel launch per step (the
+    aero-map sweep of src/ui/aeromap.ts:73-114 run as concurrent cases).
+    `lattices[i]` is an AeroEngine view of lattice i for voxelize/read calls."""
+
+    def __init__(self, grids, sim=None, lib=None):
+        """grids: list of (dims, origin, h)."""
+        self.lib = lib or _abi.load()
+        self.sim = sim or make_sim()
+        arr = (_abi.Grid * len(grids))()
+        for k, (dims, origin, h) in enumerate(grids):
+            arr[k].nx, arr[k].ny, arr[k].nz = [int(d) for d in dims]
+            for j in range(3):
+                arr[k].origin[j] = origin[j]
+            arr[k].h = h
+        b = ctypes.c_void_p()
+        rc = self.lib.wt_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(grids), ctypes.byref(self.sim),
+                                      ctypes.byref(b))
+        if rc != _abi.WT_OK:
+            raise _abi.WindTunnelError(rc, "wt_batch_create: " + self.lib.wt_batch_last_error(None).decode())
+        self.b = b
+        self.lattices = [AeroEngine(dims=d, origin=o, h=h, sim=self.sim, lib=self.lib,
+                                    _ctx=self.lib.wt_batch_lattice(b, k)) for k, (d, o, h) in enumerate(grids)]
+
+    def _check(self, rc, what):
+        if rc != _abi.WT_OK:
+            raise _abi.WindTunnelError(rc, f"{what}: {self.lib.wt_batch_last_error(self.b).decode()}")
+
+    def step(self, n_lbm_steps, heat_passes=0, heat_dt=0.0):
+        self._check(self.lib.wt_batch_step(self.b, int(n_lbm_steps), int(heat_passes), float(heat_dt)),
+                    "wt_batch_step")
+        for e in self.lattices:
+            e.steps_since_read += n_lbm_steps
+
+    def tune(self):
+        bx, by, ms = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_float()
+        self._check(self.lib.wt_batch_tune(self.b, ctypes.byref(bx), ctypes.byref(by), ctypes.byref(ms)),
+                    "wt_batch_tune")
+        return bx.value, by.value, ms.value
+
+    def stream(self):
+        return self.lib.wt_batch_stream(self.b)
+
+    def close(self):
+        if getattr(self, "b", None):
+            for e in self.lattices:
+                e.ctx = None
+            self.lib.wt_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

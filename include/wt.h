@@ -188,6 +188,33 @@ int wt_sync(wt_ctx* ctx);
 /* Message of the last failure on ctx (or of the last failed wt_create if ctx is NULL). */
 const char* wt_last_error(const wt_ctx* ctx);
 
+/* Autotuner: time the collide-stream kernel under each candidate block shape
+ * (cells along x by rows along y: 128x1, 64x2, 32x4, 256x1, 128x2, 64x4, 32x8)
+ * and keep the fastest.  The simulation state is saved and restored, so the
+ * lattice does not advance.  Outputs may be NULL. */
+int wt_tune(wt_ctx* ctx, uint32_t* bx, uint32_t* by, float* ms_per_step);
+
+/* ---- batches: many lattices advanced together (aero-map sweeps) -------------
+ * No single reference function: the reference runs one lattice and sweeps the
+ * aero map point by point (src/ui/aeromap.ts:73-114, re-voxelizing per point
+ * through engine.ts:469).  A batch holds `count` lattices of any sizes with the
+ * same simulation parameters; one kernel launch per LBM step covers every
+ * lattice's blocks, and the launches of a wt_batch_step call are captured once
+ * into a CUDA graph and replayed.  Each lattice is an ordinary wt_ctx
+ * (wt_batch_lattice): voxelize, reset, read forces and fields with the single-
+ * lattice calls; do not wt_destroy it. */
+typedef struct wt_batch wt_batch;
+int wt_batch_create(const wt_grid* grids, uint32_t count, const wt_sim* sim, wt_batch** out);
+int wt_batch_destroy(wt_batch* batch);
+uint32_t wt_batch_count(const wt_batch* batch);
+wt_ctx* wt_batch_lattice(wt_batch* batch, uint32_t index);
+/* n_lbm_steps / heat_passes / heat_dt as wt_step, for every lattice. */
+int wt_batch_step(wt_batch* batch, int n_lbm_steps, int heat_passes, float heat_dt);
+/* Autotuner over the block shapes for the whole batch (state saved and restored). */
+int wt_batch_tune(wt_batch* batch, uint32_t* bx, uint32_t* by, float* ms_per_step);
+void* wt_batch_stream(wt_batch* batch);
+const char* wt_batch_last_error(const wt_batch* batch);
+
 /* Library version, e.g. "libwt 0.1 sm_103a". */
 const char* wt_version(void);
 
