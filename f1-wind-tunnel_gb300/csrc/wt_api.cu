@@ -789,13 +789,23 @@ int bfail(wt_batch* b, int code, const std::string& m) {
   } while (0)
 
 uint64_t batch_version(const wt_batch* b) {
-  uint64_t v = 0;
+  uint64_t v = ((uint64_t)b->bx << 32) ^ ((uint64_t)b->by << 48);
   for (auto* c : b->lat) v = v * 1000003ull + c->version + ((uint64_t)c->bx << 40) + ((uint64_t)c->by << 52);
   return v;
 }
 
 // Device tables (per-lattice step arguments, block ranges, reduction records).
+// Every member first takes the batch's block shape (the launch uses b->bx x b->by
+// for all lattices, and each member's block map and per-warp buffers are sized
+// for its own shape); only then is the table version compared.
 int refresh_batch(wt_batch* b) {
+  for (auto* c : b->lat) {
+    if (c->bx != b->bx || c->by != b->by) {
+      int rc = set_geometry(c, b->bx, b->by);
+      if (rc) return bfail(b, rc, c->err);
+      if (c->bx != b->bx || c->by != b->by) return bfail(b, WT_ERR_ARG, "batch block shape not accepted");
+    }
+  }
   const uint64_t v = batch_version(b);
   if (v == b->version) return WT_OK;
   const size_t count = b->lat.size();
@@ -805,10 +815,6 @@ int refresh_batch(wt_batch* b) {
   uint32_t base = 0, cap = WT_PENDING_MAX;
   for (size_t i = 0; i < count; i++) {
     wt_ctx* c = b->lat[i];
-    if (c->bx != b->bx || c->by != b->by) {
-      int rc = set_geometry(c, b->bx, b->by);
-      if (rc) return bfail(b, rc, c->err);
-    }
     args[i] = step_args(c);
     tiles[i].base = base;
     tiles[i].gx = c->geom.grid.x;
@@ -831,6 +837,8 @@ int refresh_batch(wt_batch* b) {
 cudaError_t enqueue_batch(wt_batch* b, int n, int heat_passes, float dt, cudaStream_t s) {
   const uint32_t count = (uint32_t)b->lat.size();
   const dim3 block(b->bx, b->by, 1);
+  for (auto* c : b->lat)  // the tables were built for exactly this shape
+    if (c->geom.block.x != block.x || c->geom.block.y != block.y) return cudaErrorInvalidConfiguration;
   uint32_t pending = 0;
   for (int k = 0; k < n; k++) {
     const bool last = (k == n - 1);

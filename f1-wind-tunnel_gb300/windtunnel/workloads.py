@@ -89,3 +89,29 @@ def bytes_per_lup(storage):
 
 
 HEAT_BYTES_PER_CELL = 28  # fields 16 + emit 4 + tin 4 read, tout 4 written
+
+
+def f1_large_config(storage="f32", seed=0):
+    """The precision-sweep lattice: the same F1 at 512x192x160 (15.7 M cells), h = 2.25 cm."""
+    return f1_config(dims=(512, 192, 160), h=0.0225, seed=seed, storage=storage)
+
+
+AEROMAP_RIDE_MM = (10.0, 22.5, 35.0, 47.5, 60.0)
+
+
+def aeromap_cases(seed=0, uneven=8):
+    """The batched aero map: 25 lattices 256x96x80 (front x rear ride height in
+    10-60 mm, serpentine order of src/ui/aeromap.ts:79-84, re-voxelized per case)
+    plus `uneven` lattices whose sizes run linearly from 128x48x40 to 384x144x120
+    over the same 11.52 m tunnel.  Returns [(dims, origin, h, shape, label)]."""
+    from .sweep import aero_map_points
+    out = []
+    for p in aero_map_points(AEROMAP_RIDE_MM, AEROMAP_RIDE_MM):
+        shape = config_f1_shape(seed, ride=p.front, rear_ride=p.rear)
+        out.append(((256, 96, 80), (ORIGIN_X, 0.0, 0.0), 0.045, shape, f"front {p.front*1e3:.1f} mm rear {p.rear*1e3:.1f} mm"))
+    for k in range(uneven):
+        t = k / max(1, uneven - 1)
+        nx = int(round((128 + t * 256) / 8)) * 8
+        ny, nz = nx * 3 // 8, nx * 5 // 16
+        out.append(((nx, ny, nz), (ORIGIN_X, 0.0, 0.0), 11.52 / nx, config_f1_shape(seed), f"uneven {nx}x{ny}x{nz}"))
+    return out

@@ -85,3 +85,38 @@ def test_tune_keeps_state(wt_lib, oracle_mod, golden):
     for l, s in zip(b.lattices, snap):
         np.testing.assert_array_equal(l.read_populations(), s)
     b.close()
+
+
+def test_batch_after_block_change_bitexact(wt_lib, oracle_mod, golden):
+    """Mixed lattice sizes, the batch moved to another block shape (what the tuner
+    does), then stepped: still bit-exact against the oracle."""
+    from windtunnel import AeroBatch
+    from windtunnel.engine import make_sim
+    _, man = golden
+    cs = cases(man)
+    sim = make_sim()
+    b = AeroBatch([g for g, _ in cs], sim=sim)
+    for (g, shape), e in zip(cs, b.lattices):
+        e.set_shape_raw(shape)
+    b.step(2)  # tables and graph for the default shape
+    bx, by, ms = b.tune()
+    assert bx * by <= 256
+    want = []
+    for g, shape in cs:
+        o = oracle_mod.Oracle(*g, sim)
+        o.voxelize(shape)
+        o.reset()
+        o.steps(2)
+        o.read(reset_forces=True)
+        want.append(o)
+    for e in b.lattices:
+        e.read_forces_raw()
+    b.step(8)
+    b.step(8)
+    for e, o in zip(b.lattices, want):
+        o.steps(16)
+        od = o.read(reset_forces=True)
+        np.testing.assert_array_equal(e.read_populations(), od["f"])
+        np.testing.assert_array_equal(e.debug_read()["fields"], od["fields"])
+        assert list(e.read_forces_raw().raw) == od["forces"].tolist()
+    b.close()
