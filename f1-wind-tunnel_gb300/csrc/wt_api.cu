@@ -26,6 +26,7 @@ struct wt_ctx {
   size_t elem = 4;
   StepGeom geom{};
   uint32_t sm_count = 0;
+  uint32_t prefetch_ahead = 0;  // resident step blocks at the current block shape
   // device buffers
   void* pop = nullptr;
   uint32_t* cellw = nullptr;
@@ -123,18 +124,30 @@ int dalloc(wt_ctx* c, T** p, size_t bytes) {
   return WT_OK;
 }
 
+// x-dependent base relaxation time (wgsl.ts:260).
+float tau0_at(const wt_sim& s, uint32_t nx, uint32_t x) {
+  const float fnx = (float)nx, fx = (float)x;
+  return s.tau0 + s.sponge_amp * h_smooth(fnx - s.sponge_cells, fnx - 1.0f, fx) +
+         s.inlet_amp * (1.0f - h_smooth(0.0f, s.inlet_cells, fx));
+}
+
+// Every relaxation time must be finite and >= 2^-10 (physical runs use > 0.5;
+// the collision kernel's Smagorinsky quotient relies on tau0^2 >= 2^-20).
+bool valid_tau(const wt_sim& s, uint32_t nx) {
+  for (uint32_t x = 0; x < nx; x++) {
+    const float t = tau0_at(s, nx, x);
+    if (!(t >= 0x1p-10f) || !(t < 1e30f)) return false;
+  }
+  return true;
+}
+
 // Per-parameter tables: x-dependent tau0 (wgsl.ts:260), Smagorinsky factor,
 // inlet equilibrium, belt coefficients.
 int apply_sim(wt_ctx* c) {
   const wt_sim& s = c->sim;
   std::vector<float>& t0 = c->tau_host;
   t0.resize(c->nx);
-  const float fnx = (float)c->nx;
-  for (uint32_t x = 0; x < c->nx; x++) {
-    const float fx = (float)x;
-    t0[x] = s.tau0 + s.sponge_amp * h_smooth(fnx - s.sponge_cells, fnx - 1.0f, fx) +
-            s.inlet_amp * (1.0f - h_smooth(0.0f, s.inlet_cells, fx));
-  }
+  for (uint32_t x = 0; x < c->nx; x++) t0[x] = tau0_at(s, c->nx, x);
   WT_CUDA(c, cudaMemcpyAsync(c->tau0_x, t0.data(), c->nx * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   const float K = 0x1.974b24p+4f;  // 18 * 1.41421356 evaluated as an abstract constant, rounded once
   c->ks2 = K * s.smag * s.smag;
@@ -245,6 +258,9 @@ StepArgs step_args(const wt_ctx* c) {
   memcpy(a.floor_k, c->floor_k, sizeof(a.floor_k));
   memcpy(a.feq_guard, c->feq_guard, sizeof(a.feq_guard));
   a.guard_uu = guard_threshold();
+  fill_slot_offsets(a);
+  a.prefetch_ahead = c->prefetch_ahead;
+  a.pop_bytes = 19ull * c->np * c->elem;
   return a;
 }
 
@@ -342,6 +358,7 @@ int set_geometry(wt_ctx* c, uint32_t bx, uint32_t by) {
   c->block_slot = nullptr;
   c->mass_partial = nullptr;
   c->geom = g;
+  c->prefetch_ahead = step_resident_blocks(c->sim.storage, g, c->sm_count);
   c->bx = g.block.x;
   c->by = g.block.y;
   int rc;
@@ -380,6 +397,7 @@ int create_ctx(const wt_grid* grid, const wt_sim* sim, cudaStream_t ext, wt_ctx*
   if (np * 19 >= (1ull << 32)) return fail(nullptr, WT_ERR_ARG, "wt_create: lattice too large (19 * cells must stay below 2^32)");
   if (!(grid->h > 0.0f)) return fail(nullptr, WT_ERR_ARG, "wt_create: cell size must be positive");
   if (!valid_storage(sim->storage)) return fail(nullptr, WT_ERR_ARG, "wt_create: unknown storage format");
+  if (!valid_tau(*sim, grid->nx)) return fail(nullptr, WT_ERR_ARG, "wt_create: relaxation time below 2^-10 or not finite");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(nullptr, WT_ERR_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
@@ -400,6 +418,7 @@ int create_ctx(const wt_grid* grid, const wt_sim* sim, cudaStream_t ext, wt_ctx*
   if (const char* s = getenv("WT_STEP_BX")) c->bx = (uint32_t)atoi(s);
   if (const char* s = getenv("WT_STEP_BY")) c->by = (uint32_t)atoi(s);
   c->geom = step_geometry(c->nx, c->ny, c->nz, c->bx, c->by);
+  c->prefetch_ahead = step_resident_blocks(c->sim.storage, c->geom, c->sm_count);
   c->bx = c->geom.block.x;
   c->by = c->geom.block.y;
   int rc = 0;
@@ -461,6 +480,7 @@ int wt_set_sim(wt_ctx* c, const wt_sim* sim) {
   if (rc) return rc;
   if (!sim) return fail(c, WT_ERR_ARG, "wt_set_sim: null sim");
   if (sim->storage != c->sim.storage) return fail(c, WT_ERR_ARG, "wt_set_sim: storage format is fixed at wt_create");
+  if (!valid_tau(*sim, c->nx)) return fail(c, WT_ERR_ARG, "wt_set_sim: relaxation time below 2^-10 or not finite");
   c->sim = *sim;
   return apply_sim(c);
 }

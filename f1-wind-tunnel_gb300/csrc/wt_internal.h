@@ -49,7 +49,16 @@ struct StepArgs {
   float feq_in[19];            // feq(i, 1, (u_in, 0, 0))
   float floor_k[19];           // 6 * w_i * c_ix (belt term coefficient)
   float feq_guard[19];         // feq(i, 1, (u_in/2, 0, 0)): the divergence guard's reset state
+  // Slot offsets relative to the cell index, modulo 2^32 (19 * np < 2^32):
+  uint32_t own_ofs[19];        // i * np:                  pop[i][x]
+  uint32_t pull_ofs[19];       // opp(i) * np - off(c_i):  pop[opp(i)][x - c_i]
+  uint32_t push_ofs[19];       // i * np + off(c_i):       pop[i][x + c_i]
+  uint32_t prefetch_ahead;     // blocks ahead whose rows a block prefetches into L2 (0: none)
+  uint64_t pop_bytes;          // size of the population allocation
 };
+
+// Fills own_ofs / pull_ofs / push_ofs from nx, ny, np.
+void fill_slot_offsets(StepArgs& a);
 
 struct HeatArgs {
   const float4* fields;
@@ -67,6 +76,8 @@ struct StepGeom {
 };
 
 StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx, uint32_t by);
+// Blocks of the collide-stream kernel resident on the whole device at this block shape.
+uint32_t step_resident_blocks(uint32_t storage, const StepGeom& g, uint32_t sm_count);
 
 // Block ranges of the lattices of a batch launch (see batch_step_kernel).
 struct BatchTiles {

@@ -52,6 +52,17 @@ __device__ __forceinline__ void sfor(F&& f) {
   sfor_impl(std::make_integer_sequence<int, N>{}, f);
 }
 
+// a / b from r = RN(1/b) by Markstein's correction step (P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990): q = RN(a r) lies within one ulp of a/b, the remainder
+// e = a - q b is exact under a fused multiply-add, and RN(q + e r) = RN(a/b).
+// The remainder stays exact (a multiple of 2^-149 at worst) and q normal for
+// |a| >= 2^-60 or a = 0 with b in [2^-14, 2^14]; callers keep to that range.
+__device__ __forceinline__ float div_rcp(float a, float b, float r) {
+  const float q = __fmul_rn(a, r);
+  return __fmaf_rn(__fmaf_rn(-q, b, a), r, q);
+}
+
 // Population storage.  F32 keeps f_i; F16/BF16 keep f_i - w_i, which is small
 // and keeps the significant bits of the deviation from rest.
 struct StoreF32 {
@@ -63,14 +74,19 @@ struct StoreF32 {
 };
 // F16 keeps (f_i - w_i) * 2^14: the deviations (~1e-2 and below) then stay in
 // half's normal range down to ~4e-9 instead of turning subnormal below 6e-5;
-// the power-of-two scale adds no rounding.
+// the power-of-two scale adds no rounding.  Both conversions are single fused
+// multiply-adds with the same bits as the separate operations: h * 2^-14 and
+// v * 2^14, w * 2^14 are exact, so fma(h, 2^-14, w) = RN(w + h 2^-14) and
+// fma(v, 2^14, -w 2^14) = RN(2^14 (v - w)) = 2^14 RN(v - w) (|v| < 2^100).
 constexpr float F16_SCALE = 16384.0f, F16_INV = 1.0f / 16384.0f;
 struct StoreF16 {
   typedef __half T;
   static constexpr uint32_t id = 1;
-  __device__ __forceinline__ static float ld(const T* p, float w) { return w + __half2float(__ldg(p)) * F16_INV; }
-  __device__ __forceinline__ static float ld_smem(const T* p, float w) { return w + __half2float(*p) * F16_INV; }
-  __device__ __forceinline__ static void st(T* p, float v, float w) { *p = __float2half_rn((v - w) * F16_SCALE); }
+  __device__ __forceinline__ static float ld(const T* p, float w) { return __fmaf_rn(__half2float(__ldg(p)), F16_INV, w); }
+  __device__ __forceinline__ static float ld_smem(const T* p, float w) { return __fmaf_rn(__half2float(*p), F16_INV, w); }
+  __device__ __forceinline__ static void st(T* p, float v, float w) {
+    *p = __float2half_rn(__fmaf_rn(v, F16_SCALE, -(w * F16_SCALE)));
+  }
 };
 struct StoreBF16 {
   typedef __nv_bfloat16 T;

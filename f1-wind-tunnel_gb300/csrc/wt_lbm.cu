@@ -89,7 +89,21 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
     if constexpr (CZd(i) < 0) mz = mz - f[i];
   });
   const float den = (rho < 1e-4f) ? 1e-4f : rho;
-  float ux = mx / den, uy = my / den, uz = mz / den;
+  // u = m / den with one correctly rounded reciprocal and Markstein corrections:
+  // the quotients only matter for rho in [0.3, 3] (any other rho takes the guard
+  // below), where they equal IEEE division for |m| >= 2^-60 or m = 0; a warp
+  // holding a smaller nonzero numerator takes IEEE division (no such state
+  // arises from populations near w_i, whose sums are multiples of ~2^-30).
+  float rcp = __frcp_rn(den);
+  float ux = div_rcp(mx, den, rcp), uy = div_rcp(my, den, rcp), uz = div_rcp(mz, den, rcp);
+  {
+    const uint32_t small = min(min((__float_as_uint(mx) & 0x7fffffffu) - 1u, (__float_as_uint(my) & 0x7fffffffu) - 1u),
+                               (__float_as_uint(mz) & 0x7fffffffu) - 1u);  // zero -> 0xffffffff
+    const bool tiny = small < 0x21800000u - 1u;                             // 0 < |m| < 2^-60
+    if (__any_sync(__activemask(), tiny) && tiny) {
+      ux = __fdiv_rn(mx, den); uy = __fdiv_rn(my, den); uz = __fdiv_rn(mz, den);
+    }
+  }
   float g[19];
   // length(u) > 0.35 (wgsl.ts:238) <=> u.u > guard_uu: sqrt is correctly rounded and
   // monotonic, and guard_uu is the largest float whose square root rounds to <= 0.35f.
@@ -99,6 +113,7 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
   // equilibria are the same for every cell and come precomputed from the host.
   if (guard) {
     rho = 1.0f;
+    rcp = 1.0f;
     ux = u_in * 0.5f; uy = 0.0f; uz = 0.0f;
   }
   sfor<19>([&](auto I) { g[I] = guard ? feq_guard[I] : f[I]; });
@@ -139,7 +154,10 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
     if constexpr (cy * cz < 0) pyz = pyz - ne;
   });
   const float q = __fsqrt_rn(pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
-  const float tau = 0.5f * (tau0 + __fsqrt_rn(tau0 * tau0 + __fdiv_rn(ks2 * q, rho)));
+  // ks2 q / rho with rho in [0.3, 3] (or 1 after the guard) and rcp = RN(1/rho):
+  // IEEE-exact for ks2 q >= 2^-60; below that the quotient (< 2^-58) vanishes in
+  // tau0^2 + quotient (tau0 >= 2^-10 is enforced by the API), as the exact one does.
+  const float tau = 0.5f * (tau0 + __fsqrt_rn(tau0 * tau0 + div_rcp(ks2 * q, rho, rcp)));
   const float omega = __frcp_rn(tau);  // correctly rounded 1/tau, the same bits as 1.0f / tau
   const float c1 = (1.0f - omega) * 4.5f;
   const float k0 = c1 * Wd(0), k1 = c1 * Wd(1), k2 = c1 * Wd(7);
@@ -208,10 +226,63 @@ __device__ __forceinline__ void link_force(float v, uint32_t group, float (&gf)[
 // ---------------------------------------------------------------------------
 constexpr uint32_t TILE = 128;
 
+// Slot offsets of direction i relative to the cell index (mod 2^32): the
+// single-lattice kernel reads the host-computed tables straight from its
+// parameter block; the batch kernel, whose arguments sit in global memory,
+// computes them from np, nx, nx*ny.
+struct OfsTable {
+  static constexpr bool plain_path = true;
+  const StepArgs& a;
+  template <int i, class PT> __device__ __forceinline__ PT* own_at(PT* P, uint32_t idx) const {
+    return P + (idx + a.own_ofs[i]);
+  }
+  template <int i> __device__ __forceinline__ uint32_t pull() const { return a.pull_ofs[i]; }
+  template <int i> __device__ __forceinline__ uint32_t push() const { return a.push_ofs[i]; }
+};
+// The batch kernel keeps the two-way (interior / face) gather: with a third,
+// plain-neighbour copy of the 19 accesses its argument loads from global memory
+// are hoisted and spill (~400 B per thread).
+struct OfsCalc {
+  static constexpr bool plain_path = false;
+  uint32_t np;
+  template <int i, class PT> __device__ __forceinline__ PT* own_at(PT* P, uint32_t idx) const {
+    return P + (size_t)i * np + idx;
+  }
+  template <int i> __device__ __forceinline__ uint32_t pull() const { return 0u; }
+  template <int i> __device__ __forceinline__ uint32_t push() const { return 0u; }
+};
+
+// L2 prefetch of the tile a.prefetch_ahead blocks further on (about one wave of
+// resident blocks ahead, in launch order): thread t < 19 * by issues one bulk
+// prefetch of direction t % 19 over row t / 19 of that tile, so DRAM streams the
+// next wave's own-cell rows while this wave computes.  The byte range is
+// widened to 16-byte boundaries and clipped to the population allocation.
+template <class T>
+__device__ __forceinline__ void prefetch_tile(const StepArgs& a, uint3 bid, uint3 gdim) {
+  if (a.prefetch_ahead == 0) return;
+  const uint32_t nb = gdim.x * gdim.y * gdim.z;
+  const uint32_t tb = bid.x + gdim.x * (bid.y + gdim.y * bid.z) + a.prefetch_ahead;
+  const uint32_t t = threadIdx.x + blockDim.x * threadIdx.y;
+  if (tb >= nb || t >= 19u * blockDim.y) return;
+  const uint32_t dir = t % 19u, row = t / 19u;
+  const uint32_t tx = tb % gdim.x, ty = (tb / gdim.x) % gdim.y, tz = tb / (gdim.x * gdim.y);
+  const uint32_t y = ty * blockDim.y + row, x0 = tx * blockDim.x;
+  if (y >= a.ny || x0 >= a.nx) return;
+  const uint32_t cells = min(blockDim.x, a.nx - x0);
+  const uint64_t e0 = (uint64_t)dir * a.np + x0 + (uint64_t)a.nx * (y + (uint64_t)a.ny * tz);
+  const uint64_t b0 = (e0 * sizeof(T)) & ~15ull;
+  uint64_t b1 = ((e0 + cells) * sizeof(T) + 15ull) & ~15ull;
+  if (b1 > a.pop_bytes) b1 = a.pop_bytes & ~15ull;
+  if (b1 <= b0) return;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<const char*>(a.pop) + b0),
+               "r"((uint32_t)(b1 - b0))
+               : "memory");
+}
+
 // One block's cells of one lattice.  bid/gdim are the block coordinates and grid
 // of that lattice's tiling; slots is where this step's force records go.
-template <class St, bool GATHER, bool FIELDS>
-__device__ __forceinline__ void step_tile(const StepArgs& a, ForceSlot* slots, uint3 bid, uint3 gdim) {
+template <class St, bool GATHER, bool FIELDS, class Ofs>
+__device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, ForceSlot* slots, uint3 bid, uint3 gdim) {
   const uint8_t* __restrict__ solid_u8 = a.solid;
   const uint32_t nx = a.nx, ny = a.ny, nz = a.nz;
   const uint32_t x = bid.x * blockDim.x + threadIdx.x;
@@ -220,26 +291,49 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, ForceSlot* slots, u
   const bool in = (x < nx) && (y < ny);
   const uint32_t nxy = nx * ny;
   const uint32_t np = (uint32_t)a.np;
+  if constexpr (Ofs::plain_path) prefetch_tile<typename St::T>(a, bid, gdim);
   const uint32_t idx = in ? x + nx * y + nxy * z : 0u;
   const uint32_t cw = in ? __ldg(a.cellw + idx) : CW_SOLID;
+  typedef typename St::T PT;
+  PT* __restrict__ P = reinterpret_cast<PT*>(a.pop);
   float gf[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   float rho_cell = 0.0f;
   bool guard = false;
+  // A warp is 32 consecutive x of one (y, z) row (block widths are multiples of
+  // 32), so the y/z faces are warp-uniform: those rows take the full boundary
+  // path.  The x faces (inlet x = 0, outlet x = nx - 1) stay in the interior
+  // paths: their out-of-domain directions still load an in-bounds slot (the
+  // row wraps into the previous / next row of the same direction array), the
+  // value is then replaced by the inlet / outlet population, and their
+  // discarded pushes land in slots the next step never reads (the outlet and
+  // inlet directions of x = nx - 1 and x = 0 cells).  No warp diverges on them.
+  const bool yzface = (y == 0) | (y == ny - 1) | (z == 0) | (z == nz - 1);
+  // Warp-uniform plain test (all lanes converged here): no fluid lane of this
+  // warp has a bounce-back link, so every population moves between plain
+  // neighbour slots.
+  const bool plain = Ofs::plain_path &&
+      __all_sync(0xffffffffu, !in || (cw & CW_SOLID) || (!yzface && (cw & CW_LINKS) == 0u));
 
   if (in && (cw & CW_SOLID)) {
     if constexpr (!GATHER) {  // wgsl.ts:183: solid cells hold w_i
-      sfor<19>([&](auto K) { stp<St>(a.pop, K, np, idx, Wd(K), K); });
+      if constexpr (Ofs::plain_path) sfor<19>([&](auto K) { St::st(ofs.template own_at<K>(P, idx), Wd(K), Wd(K)); });
+      else sfor<19>([&](auto K) { stp<St>(a.pop, K, np, idx, Wd(K), K); });
     }
     if constexpr (FIELDS) a.fields[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
   } else if (in) {
-    const bool face = (x == 0) | (x == nx - 1) | (y == 0) | (y == ny - 1) | (z == 0) | (z == nz - 1);
     float f[19], fo[19];
     float4 pu = make_float4(0.f, 0.f, 0.f, 0.f);
     if (x == nx - 1) pu = a.outlet_u[y + ny * z];
     const float floor_u = (cw & CW_BELT) ? 0.0f : a.u_in;
 
     // ---------------------------------------------------------------- gather
-    if (!face) {
+    if (plain) {
+      sfor<19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (GATHER) f[i] = St::ld(P + (idx + ofs.template pull<i>()), Wd(i));
+        else f[i] = St::ld(ofs.template own_at<i>(P, idx), Wd(i));
+      });
+    } else if (!yzface) {
       sfor<19>([&](auto I) {
         constexpr int i = I;
         if constexpr (i == 0) {
@@ -288,6 +382,22 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, ForceSlot* slots, u
         }
       });
     }
+    if (!yzface) {  // inlet / outlet directions of the x-face lanes (wgsl.ts:207-210)
+      if (x == 0) {
+        sfor<19>([&](auto I) {
+          if constexpr (CXd(I) > 0) f[I] = a.feq_in[I];
+        });
+      }
+      if ((x | 31u) >= nx - 1) {  // warp-uniform: this warp holds the outlet column
+        sfor<19>([&](auto I) {
+          constexpr int i = I;
+          if constexpr (CXd(i) < 0) {
+            const float e = feq_rho1<i>(pu.x, pu.y, pu.z);
+            f[i] = (x == nx - 1) ? e : f[i];
+          }
+        });
+      }
+    }
 
     // ---------------------------------------------------------------- forces
     if (cw & CW_FORCE) {
@@ -320,9 +430,15 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, ForceSlot* slots, u
     if constexpr (!GATHER) {
       sfor<19>([&](auto J) {
         constexpr int j = J;
-        stp<St>(a.pop, OPPd(j), np, idx, fo[j], j);
+        if constexpr (Ofs::plain_path) St::st(ofs.template own_at<OPPd(j)>(P, idx), fo[j], Wd(j));
+        else stp<St>(a.pop, OPPd(j), np, idx, fo[j], j);
       });
-    } else if (!face) {
+    } else if (plain) {
+      sfor<19>([&](auto J) {
+        constexpr int j = J;
+        St::st(P + (idx + ofs.template push<j>()), fo[j], Wd(j));
+      });
+    } else if (!yzface) {
       sfor<19>([&](auto J) {
         constexpr int j = J;
         if constexpr (j == 0) {
@@ -380,7 +496,13 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, ForceSlot* slots, u
   if (slot < 0) return;  // no force-carrying link in this block: no barrier, no record
   __shared__ double s_f[9][8];
   __shared__ int32_t s_r[6][8];
-  {
+  bool any_force = false;
+#pragma unroll
+  for (int q = 0; q < 9; q++) any_force |= (gf[q] != 0.0f);
+  if (!__any_sync(0xffffffffu, any_force)) {  // no force in this warp: zero record, no FP64 shuffles
+    if (lane < 9) s_f[lane][warp] = 0.0;
+    if (lane < 6) s_r[lane][warp] = 0;
+  } else {
     double d[9];
     int32_t r[6];
 #pragma unroll
@@ -420,9 +542,35 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, ForceSlot* slots, u
   }
 }
 
+// Consecutive collide-stream launches are chained by programmatic dependent
+// launch: each grid lets the next one be scheduled as soon as all of its own
+// blocks are resident (launch_dependents), and every grid waits for its
+// predecessor to complete and flush (wait) before it touches memory, so the next
+// step's blocks are already on the SMs when the previous step retires.
+__device__ __forceinline__ void chain_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <class K, class... Args>
+cudaError_t launch_chained(K kernel, dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <class St, bool GATHER, bool FIELDS>
 __global__ void __launch_bounds__(256, 4) step_kernel(StepArgs a) {
-  step_tile<St, GATHER, FIELDS>(a, a.slots, blockIdx, make_uint3(gridDim.x, gridDim.y, gridDim.z));
+  chain_enter();
+  step_tile<St, GATHER, FIELDS>(a, OfsTable{a}, a.slots, blockIdx, make_uint3(gridDim.x, gridDim.y, gridDim.z));
 }
 
 // Many lattices in one launch: block b belongs to the lattice L with
@@ -431,6 +579,7 @@ template <class St, bool GATHER, bool FIELDS>
 __global__ void __launch_bounds__(256, 4) batch_step_kernel(const StepArgs* __restrict__ args,
                                                             const BatchTiles* __restrict__ tiles, uint32_t count,
                                                             uint32_t pending) {
+  chain_enter();
   const uint32_t b = blockIdx.x;
   uint32_t lo = 0, hi = count;  // binary search: largest L with base[L] <= b
   while (hi - lo > 1) {
@@ -443,7 +592,8 @@ __global__ void __launch_bounds__(256, 4) batch_step_kernel(const StepArgs* __re
   const uint3 gdim = make_uint3(tl.gx, tl.gy, tl.gz);
   const uint3 bid = make_uint3(t % tl.gx, (t / tl.gx) % tl.gy, t / (tl.gx * tl.gy));
   const StepArgs& a = args[lo];
-  step_tile<St, GATHER, FIELDS>(a, a.slots + (size_t)pending * a.nslots, bid, gdim);
+  const OfsCalc ofs{(uint32_t)a.np};
+  step_tile<St, GATHER, FIELDS>(a, ofs, a.slots + (size_t)pending * a.nslots, bid, gdim);
 }
 
 // Canonical initial state (LBM_INIT, wgsl.ts:147-155): f*_j = feq_j(1, (u_in,0,0))
@@ -602,26 +752,23 @@ __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceA
 template <class St>
 cudaError_t launch_step_t(bool gather, bool fields, const StepGeom& g, const StepArgs& a, cudaStream_t s) {
   if (gather) {
-    if (fields) step_kernel<St, true, true><<<g.grid, g.block, 0, s>>>(a);
-    else step_kernel<St, true, false><<<g.grid, g.block, 0, s>>>(a);
-  } else {
-    if (fields) step_kernel<St, false, true><<<g.grid, g.block, 0, s>>>(a);
-    else step_kernel<St, false, false><<<g.grid, g.block, 0, s>>>(a);
+    if (fields) return launch_chained(step_kernel<St, true, true>, g.grid, g.block, s, a);
+    return launch_chained(step_kernel<St, true, false>, g.grid, g.block, s, a);
   }
-  return cudaGetLastError();
+  if (fields) return launch_chained(step_kernel<St, false, true>, g.grid, g.block, s, a);
+  return launch_chained(step_kernel<St, false, false>, g.grid, g.block, s, a);
 }
 
 template <class St>
 cudaError_t launch_batch_t(bool gather, bool fields, dim3 block, uint32_t total_blocks, const StepArgs* args,
                            const BatchTiles* tiles, uint32_t count, uint32_t pending, cudaStream_t s) {
+  const dim3 grid(total_blocks);
   if (gather) {
-    if (fields) batch_step_kernel<St, true, true><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
-    else batch_step_kernel<St, true, false><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
-  } else {
-    if (fields) batch_step_kernel<St, false, true><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
-    else batch_step_kernel<St, false, false><<<total_blocks, block, 0, s>>>(args, tiles, count, pending);
+    if (fields) return launch_chained(batch_step_kernel<St, true, true>, grid, block, s, args, tiles, count, pending);
+    return launch_chained(batch_step_kernel<St, true, false>, grid, block, s, args, tiles, count, pending);
   }
-  return cudaGetLastError();
+  if (fields) return launch_chained(batch_step_kernel<St, false, true>, grid, block, s, args, tiles, count, pending);
+  return launch_chained(batch_step_kernel<St, false, false>, grid, block, s, args, tiles, count, pending);
 }
 
 // Host copy of feq(i, 1, (u, 0, 0)) with the reference's operation order
@@ -648,6 +795,31 @@ cudaError_t by_storage(uint32_t storage, F&& f) {
 }
 
 }  // namespace
+
+// Prefetch distance of the collide-stream kernel: one wave of resident blocks for
+// f32 storage; 0 (off) for f16/bf16, where the extra L2 traffic measured slower
+// (34.3 -> 30.4 GLUPS on the 256x96x80 F1) while f32 gained (77.5 -> 79.8 % of
+// the HBM roofline on the 512x192x160 F1).
+uint32_t step_resident_blocks(uint32_t storage, const StepGeom& g, uint32_t sm_count) {
+  if (storage != WT_STORE_F32) return 0;
+  int per_sm = 0;
+  const int threads = (int)(g.block.x * g.block.y);
+  cudaError_t e = by_storage(storage, [&](auto st) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel<decltype(st), true, false>, threads, 0);
+  });
+  if (e != cudaSuccess || per_sm <= 0) return 0;
+  return (uint32_t)per_sm * sm_count;
+}
+
+void fill_slot_offsets(StepArgs& a) {
+  const uint32_t np = (uint32_t)a.np, nx = a.nx, nxy = a.nx * a.ny;
+  for (int i = 0; i < 19; i++) {
+    const uint32_t off = (uint32_t)CXd(i) + (uint32_t)CYd(i) * nx + (uint32_t)CZd(i) * nxy;  // mod 2^32
+    a.own_ofs[i] = (uint32_t)i * np;
+    a.pull_ofs[i] = (uint32_t)OPPd(i) * np - off;
+    a.push_ofs[i] = (uint32_t)i * np + off;
+  }
+}
 
 // Block shape (bx cells along x) x (by rows along y); bx a multiple of 32 and
 // bx * by <= 256 (the kernels' launch bounds).  The autotuner picks the shape.

@@ -155,6 +155,12 @@ def test_errors_are_reported(wt_lib):
         e.set_shape_raw(s)
     with pytest.raises(WindTunnelError):
         AeroEngine(dims=(4, 1, 1), h=0.1)
+    from windtunnel.engine import make_sim
+    with pytest.raises(WindTunnelError, match="relaxation time"):
+        e.set_sim(make_sim(tau0=1e-4, sponge_amp=0.0, inlet_amp=0.0))
+    with pytest.raises(WindTunnelError, match="relaxation time"):
+        AeroEngine(dims=(16, 8, 8), h=0.1, sim=make_sim(tau0=float("nan")))
+    e.step(2)  # the rejected parameters left the context usable
     e.close()
 
 
