@@ -661,6 +661,36 @@ int wt_reset_from(wt_ctx* c, const float* u_rho, uint32_t cx, uint32_t cy, uint3
   return WT_OK;
 }
 
+int wt_read_coarse(wt_ctx* c, uint32_t cx, uint32_t cy, uint32_t cz, float* u_rho) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!u_rho || cx == 0 || cy == 0 || cz == 0 || cx > c->nx || cy > c->ny || cz > c->nz)
+    return fail(c, WT_ERR_ARG, "wt_read_coarse: coarse grid must be non-empty and no finer than the lattice");
+  float4* tmp = nullptr;
+  const size_t bytes = (size_t)cx * cy * cz * 16;
+  WT_CUDA(c, cudaMallocAsync((void**)&tmp, bytes, c->stream));
+  WT_CUDA(c, launch_coarse_average(c->fields, c->cellw, c->nx, c->ny, c->nz, tmp, cx, cy, cz, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(u_rho, tmp, bytes, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaFreeAsync(tmp, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int wt_sdf_sample(const wt_shape* shape, const wt_grid* grid, float* out) {
+  if (!shape || !grid || !out || grid->nx == 0 || grid->ny == 0 || grid->nz == 0 || !(grid->h > 0.0f))
+    return fail(nullptr, WT_ERR_ARG, "wt_sdf_sample: invalid argument");
+  if (shape->kind == 4 || shape->kind == 5 || shape->kind > WT_KIND_BOX)
+    return fail(nullptr, WT_ERR_UNSUPPORTED, "wt_sdf_sample: scene kind not built");
+  const size_t bytes = (size_t)grid->nx * grid->ny * grid->nz * 4;
+  float* tmp = nullptr;
+  cudaError_t e = cudaMalloc((void**)&tmp, bytes);
+  if (e == cudaSuccess) e = launch_sdf_sample(*shape, *grid, tmp, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, tmp, bytes, cudaMemcpyDeviceToHost);
+  if (tmp) cudaFree(tmp);
+  if (e != cudaSuccess) return fail(nullptr, WT_ERR_CUDA, std::string("wt_sdf_sample: ") + cudaGetErrorString(e));
+  return WT_OK;
+}
+
 int wt_info_get(wt_ctx* c, wt_info* out) {
   if (!c || !out) return WT_ERR_ARG;
   out->cells = c->n;

@@ -111,6 +111,11 @@ cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t
                                 cudaStream_t s);
 cudaError_t launch_read_pop(uint32_t storage, const void* pop, float* out, uint32_t n, uint64_t np, cudaStream_t s);
 cudaError_t launch_write_pop(uint32_t storage, const float* in, void* pop, uint32_t n, uint64_t np, cudaStream_t s);
+// Box average of the fluid cells' (ux, uy, uz, rho) onto a cx x cy x cz grid
+// (fine cell i of an axis belongs to coarse cell i * c / n); boxes without fluid
+// give (0, 0, 0, 1).
+cudaError_t launch_coarse_average(const float4* fields, const uint32_t* cellw, uint32_t nx, uint32_t ny, uint32_t nz,
+                                  float4* coarse, uint32_t cx, uint32_t cy, uint32_t cz, cudaStream_t s);
 cudaError_t launch_resample_init(uint32_t storage, const float4* coarse, uint32_t cx, uint32_t cy, uint32_t cz,
                                  void* pop, float4* fields, float4* outlet_u, uint32_t nx, uint32_t ny, uint32_t nz,
                                  uint64_t np, cudaStream_t s);
@@ -118,6 +123,7 @@ cudaError_t launch_resample_init(uint32_t storage, const float4* coarse, uint32_
 // wt_voxel.cu
 cudaError_t launch_voxelize(const wt_shape& shape, const wt_grid& grid, uint8_t* solid, float* emit,
                             cudaStream_t s);
+cudaError_t launch_sdf_sample(const wt_shape& shape, const wt_grid& grid, float* out, cudaStream_t s);
 cudaError_t launch_cell_words(const uint8_t* solid, const float* emit, uint32_t* cellw, uint32_t nx, uint32_t ny,
                               uint32_t nz, cudaStream_t s);
 cudaError_t launch_block_flags(const uint32_t* cellw, const StepGeom& g, uint32_t nx, uint32_t ny, uint32_t nz,
@@ -128,5 +134,8 @@ cudaError_t launch_solid_from_u32(const uint32_t* in, uint8_t* solid, uint64_t n
 
 // wt_heat.cu
 cudaError_t launch_heat(const HeatArgs& a, cudaStream_t s);
+
+// wt_conv.cu: last error of the calling thread in the network operators (wt_net.h)
+std::string& net_error();
 
 }  // namespace wt

@@ -666,6 +666,31 @@ __global__ void resample_kernel(const float4* coarse, uint32_t cx, uint32_t cy, 
   if (x == nx - 1) outlet_u[y + ny * z] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
 
+// Coarse box average of the fluid cells (the inverse direction of resample_kernel).
+__global__ void coarse_average_kernel(const float4* __restrict__ fields, const uint32_t* __restrict__ cellw,
+                                      uint32_t nx, uint32_t ny, uint32_t nz, float4* __restrict__ coarse, uint32_t cx,
+                                      uint32_t cy, uint32_t cz) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cx * cy * cz) return;
+  const uint32_t a = i % cx, b = (i / cx) % cy, c = i / (cx * cy);
+  const uint32_t x0 = (uint32_t)((uint64_t)a * nx / cx), x1 = (uint32_t)((uint64_t)(a + 1) * nx / cx);
+  const uint32_t y0 = (uint32_t)((uint64_t)b * ny / cy), y1 = (uint32_t)((uint64_t)(b + 1) * ny / cy);
+  const uint32_t z0 = (uint32_t)((uint64_t)c * nz / cz), z1 = (uint32_t)((uint64_t)(c + 1) * nz / cz);
+  double sx = 0.0, sy = 0.0, sz = 0.0, sr = 0.0;
+  uint32_t cnt = 0;
+  for (uint32_t z = z0; z < z1; z++)
+    for (uint32_t y = y0; y < y1; y++)
+      for (uint32_t x = x0; x < x1; x++) {
+        const uint32_t idx = x + nx * (y + ny * z);
+        if (cellw[idx] & CW_SOLID) continue;
+        const float4 f = fields[idx];
+        sx += f.x; sy += f.y; sz += f.z; sr += f.w;
+        cnt++;
+      }
+  coarse[i] = cnt ? make_float4((float)(sx / cnt), (float)(sy / cnt), (float)(sz / cnt), (float)(sr / cnt))
+                  : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+}
+
 // Deterministic reduction of the pending steps' partial records: block s < nsteps
 // sums step s's records (each thread a fixed strided subset with all 15
 // components in registers, then a fixed shuffle tree and the warps in order)
@@ -878,6 +903,13 @@ cudaError_t launch_write_pop(uint32_t storage, const float* in, void* pop, uint3
     write_pop_kernel<decltype(st)><<<(n + 255) / 256, 256, 0, s>>>(in, pop, n, (uint32_t)np);
     return cudaGetLastError();
   });
+}
+
+cudaError_t launch_coarse_average(const float4* fields, const uint32_t* cellw, uint32_t nx, uint32_t ny, uint32_t nz,
+                                  float4* coarse, uint32_t cx, uint32_t cy, uint32_t cz, cudaStream_t s) {
+  const uint32_t n = cx * cy * cz;
+  coarse_average_kernel<<<(n + 127) / 128, 128, 0, s>>>(fields, cellw, nx, ny, nz, coarse, cx, cy, cz);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_resample_init(uint32_t storage, const float4* coarse, uint32_t cx, uint32_t cy, uint32_t cz,

@@ -469,7 +469,18 @@ __global__ void solid_from_u32_kernel(const uint32_t* __restrict__ in, uint8_t* 
 
 }  // namespace
 
-cudaError_t launch_voxelize(const wt_shape& shape, const wt_grid& grid, uint8_t* solid, float* emit, cudaStream_t s) {
+// Scene distance at the cell centres of `grid` (the first component of sceneSdf).
+__global__ void sdf_sample_kernel(Scene S, uint32_t nx, uint32_t ny, uint32_t nz, float ox, float oy, float oz,
+                                  float h, float* __restrict__ out) {
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+  const uint32_t z = blockIdx.z;
+  if (x >= nx || y >= ny) return;
+  const V3 p = v3(ox + ((float)x + 0.5f) * h, oy + ((float)y + 0.5f) * h, oz + ((float)z + 0.5f) * h);
+  out[x + nx * (y + ny * z)] = scene_sdf(S, p).x;
+}
+
+Scene make_scene(const wt_shape& shape) {
   Scene S;
   S.s = shape;
   // Shape-wide constants, evaluated once (same functions and operation order as per cell).
@@ -490,6 +501,20 @@ cudaError_t launch_voxelize(const wt_shape& shape, const wt_grid& grid, uint8_t*
   }
   S.rear_c = wtm::cosf(S.ang_m);
   S.rear_s = wtm::sinf(S.ang_m);
+  return S;
+}
+
+cudaError_t launch_sdf_sample(const wt_shape& shape, const wt_grid& grid, float* out, cudaStream_t s) {
+  const Scene S = make_scene(shape);
+  const dim3 block(32, 4, 1);
+  const dim3 g((grid.nx + 31) / 32, (grid.ny + 3) / 4, grid.nz);
+  sdf_sample_kernel<<<g, block, 0, s>>>(S, grid.nx, grid.ny, grid.nz, grid.origin[0], grid.origin[1], grid.origin[2],
+                                        grid.h, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_voxelize(const wt_shape& shape, const wt_grid& grid, uint8_t* solid, float* emit, cudaStream_t s) {
+  const Scene S = make_scene(shape);
   const dim3 block(32, 4, 1);
   const dim3 g((grid.nx + 31) / 32, (grid.ny + 3) / 4, grid.nz);
   voxelize_kernel<<<g, block, 0, s>>>(S, grid.nx, grid.ny, grid.nz, grid.origin[0], grid.origin[1], grid.origin[2],

@@ -100,6 +100,8 @@ _PROTOS = {
     "wt_batch_stream": (_vp, [_vp]),
     "wt_batch_last_error": (ctypes.c_char_p, [_vp]),
     "wt_version": (ctypes.c_char_p, []),
+    "wt_read_coarse": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
+    "wt_sdf_sample": (ctypes.c_int, [ctypes.POINTER(Shape), ctypes.POINTER(Grid), _vp]),
 }
 
 _lib = None

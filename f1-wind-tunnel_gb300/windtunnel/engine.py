@@ -305,6 +305,12 @@ class AeroEngine:
         assert four == 4
         self._check(self.lib.wt_reset_from(self.ctx, c.ctypes.data, cx, cy, cz), "wt_reset_from")
 
+    def read_coarse(self, cx, cy, cz):
+        """Fluid-cell box average of the last step call's (ux, uy, uz, rho): array [cz, cy, cx, 4]."""
+        out = np.empty((cz, cy, cx, 4), np.float32)
+        self._check(self.lib.wt_read_coarse(self.ctx, cx, cy, cz, out.ctypes.data), "wt_read_coarse")
+        return out
+
     def tune(self):
         """Autotune the collide-stream block shape (state is preserved); returns (bx, by, ms/step)."""
         bx, by, ms = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_float()

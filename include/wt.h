@@ -177,6 +177,19 @@ int wt_write_state(wt_ctx* ctx, const float* f, const float* u_rho, const float*
  * u_rho[4*cx*cy*cz] trilinearly resampled to the lattice; fields likewise. */
 int wt_reset_from(wt_ctx* ctx, const float* u_rho, uint32_t cx, uint32_t cy, uint32_t cz);
 
+/* Box average of the fluid cells' (ux, uy, uz, rho) of the last wt_step call's
+ * fields onto a cx x cy x cz grid (fine cell i of an axis falls in coarse cell
+ * i * c / n; boxes without fluid give (0, 0, 0, 1)); u_rho receives
+ * cx*cy*cz*4 floats, x fastest.  The training target of the warm start and the
+ * inverse direction of wt_reset_from. */
+int wt_read_coarse(wt_ctx* ctx, uint32_t cx, uint32_t cy, uint32_t cz, float* u_rho);
+
+/* Scene distance (the first component of the reference's sceneSdf,
+ * src/engine/wgsl.ts:101-116 / f1.ts:283-320) at the cell centres
+ * origin + (i + 0.5) h of `grid`; out receives nx*ny*nz floats.  Needs no
+ * context (uses the current device); the warm start's geometry input. */
+int wt_sdf_sample(const wt_shape* shape, const wt_grid* grid, float* out);
+
 int wt_info_get(wt_ctx* ctx, wt_info* out);
 
 /* The context's cudaStream_t (as void*), for callers that time or order work. */
