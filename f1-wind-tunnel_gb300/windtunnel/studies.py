@@ -1,0 +1,240 @@
+"""Measured studies of the warm start and the batched aero map.
+
+    python -m windtunnel.studies warmstart [--small] --out DIR
+        generate the training set (seeded 256x96x80 F1 runs, fields averaged
+        late in the run), train the network on the GPU with libwt's kernels and
+        save the weights.
+    python -m windtunnel.studies judge --weights FILE [--small] --out DIR
+        warm vs cold FP32 starts of held-out seeds, judged by the LBM.
+    python -m windtunnel.studies sweep --weights FILE [--small] --out DIR
+        the 25-point ride-height aero map plus 8 uneven lattices: time to 1 %
+        convergence of every case's windowed Cd and Cl, plain FP32 cold start
+        one case after another vs batched FP16 with the warm start.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import warmstart as ws
+from .surrogate import Surrogate
+from .workloads import aeromap_cases
+
+
+def log(msg):
+    print(f"[{time.strftime('%H:%M:%S')}] {msg}", flush=True)
+
+
+def dataset(seeds, settle, average_steps, every, group=64, storage="f16"):
+    """Features and time-averaged coarse targets of seeded F1 runs."""
+    shapes = [ws.case_shape(s) for s in seeds]
+    cases = [(ws.F1_DIMS, ws.F1_H, sh) for sh in shapes]
+    run = ws.run_cases(cases, settle + average_steps, warm=None, storage=storage, average=(settle, every),
+                       group=group, log=log)
+    X, M, T = [], [], []
+    for sh, coarse in zip(shapes, run["coarse"]):
+        x, m = ws.features(sh)
+        X.append(x)
+        M.append(m)
+        T.append(ws.normalize_target(coarse))
+    return np.stack(X), np.stack(T), np.stack(M), run
+
+
+def save_weights(model, path):
+    st = model.state()
+    np.savez_compressed(path, **{k: v.astype(np.float32) for k, v in st.items()})
+
+
+def load_model(path, seed=0):
+    m = Surrogate(seed=seed)
+    with np.load(path) as z:
+        m.load_state({k: z[k] for k in z.files})
+    return m
+
+
+def warm_fields(model, shapes):
+    X = np.stack([ws.features(sh)[0] for sh in shapes])
+    P = ws.predict(model, X)
+    return [ws.denormalize(p) for p in P]
+
+
+def judge(model, seeds, steps, group=64, storage="f32"):
+    """Cold and warm runs of the held-out seeds: per-seed convergence steps."""
+    shapes = [ws.case_shape(s) for s in seeds]
+    cases = [(ws.F1_DIMS, ws.F1_H, sh) for sh in shapes]
+    cold = ws.run_cases(cases, steps, storage="f32", group=group)
+    warm = ws.run_cases(cases, steps, warm=warm_fields(model, shapes), storage=storage, group=group)
+    rows = []
+    for i, s in enumerate(seeds):
+        rcd, rcl = ws.reference_values(cold["cd"][i], cold["cl"][i])
+        c = ws.convergence_step(cold["cd"][i], cold["cl"][i], rcd, rcl)
+        w = ws.convergence_step(warm["cd"][i], warm["cl"][i], rcd, rcl)
+        rows.append({"seed": int(s), "ref_cd": rcd, "ref_cl": rcl, "cold_steps": c, "warm_steps": w,
+                     "cold_steps_cd": ws.convergence_step_cd(cold["cd"][i], rcd),
+                     "warm_steps_cd": ws.convergence_step_cd(warm["cd"][i], rcd)})
+    return rows, cold, warm
+
+
+def summarize_judge(rows, horizon):
+    cold = np.array([r["cold_steps"] if r["cold_steps"] is not None else horizon for r in rows], float)
+    warm = np.array([r["warm_steps"] if r["warm_steps"] is not None else horizon for r in rows], float)
+    cold_cd = np.array([r["cold_steps_cd"] if r["cold_steps_cd"] is not None else horizon for r in rows], float)
+    warm_cd = np.array([r["warm_steps_cd"] if r["warm_steps_cd"] is not None else horizon for r in rows], float)
+    return {"cases": len(rows), "cold_mean_steps": float(cold.mean()), "warm_mean_steps": float(warm.mean()),
+            "cold_mean_steps_cd_only": float(cold_cd.mean()), "warm_mean_steps_cd_only": float(warm_cd.mean()),
+            "steps_saved_mean": float((cold - warm).mean()), "steps_saved_median": float(np.median(cold - warm)),
+            "warm_better_or_equal": int((warm <= cold).sum()),
+            "not_converged_cold": int(sum(r["cold_steps"] is None for r in rows)),
+            "not_converged_warm": int(sum(r["warm_steps"] is None for r in rows))}
+
+
+def study_warmstart(args):
+    """Training set, training, validation loss and weights (the judge is separate)."""
+    os.makedirs(args.out, exist_ok=True)
+    small = args.small
+    n_train, n_val = (16, 4) if small else (args.train_cases, args.val_cases)
+    settle, avg, every = (1200, 800, 200) if small else (args.settle, args.average, 500)
+    t0 = time.time()
+    train_seeds = list(range(1000, 1000 + n_train))
+    val_seeds = list(range(5000, 5000 + n_val))
+    log(f"generating {n_train} training + {n_val} held-out runs ({settle}+{avg} steps)")
+    Xt, Tt, Mt, run_t = dataset(train_seeds, settle, avg, every)
+    Xv, Tv, Mv, _ = dataset(val_seeds, settle, avg, every)
+    t_data = time.time() - t0
+    log(f"data done in {t_data:.1f} s; lattice step {np.mean(run_t['group_step_s']) * 1e3:.3f} ms per group step")
+    model = Surrogate(seed=0)
+    epochs = 6 if small else args.epochs
+    t1 = time.time()
+    hist = ws.train(model, Xt, Tt, Mt, epochs=epochs, batch=16 if not small else 8, lr=args.lr, log=log)
+    t_train = time.time() - t1
+    vloss = ws.validation_loss(model, Xv, Tv, Mv)
+    zero = float(((Tv) ** 2 * Mv[..., None]).sum() / max(1.0, 4 * Mv.sum()))
+    log(f"validation loss {vloss:.5f} (predicting the uniform inlet state: {zero:.5f})")
+    wpath = os.path.join(args.out, "warmstart_f1.npz")
+    save_weights(model, wpath)
+    res = {"train_cases": n_train, "val_cases": n_val, "settle_steps": settle, "average_steps": avg,
+           "data_storage": "f16", "epochs": epochs, "train_loss": hist, "val_loss": vloss,
+           "val_loss_uniform_state": zero, "data_seconds": t_data, "train_seconds": t_train,
+           "lattice_step_s_per_group": run_t["group_step_s"]}
+    with open(os.path.join(args.out, "warmstart_train.json"), "w") as f:
+        json.dump(res, f, indent=1)
+
+
+def study_judge(args):
+    """Held-out seeds: cold and warm FP32 runs judged by the LBM."""
+    os.makedirs(args.out, exist_ok=True)
+    model = load_model(args.weights)
+    seeds = list(range(5000, 5000 + (2 if args.small else args.val_cases)))
+    horizon = 4000 if args.small else args.judge_steps
+    rows, cold, warm = judge(model, seeds, horizon)
+    summary = summarize_judge(rows, horizon)
+    log(f"judge: {summary}")
+    with open(os.path.join(args.out, "warmstart_judge.json"), "w") as f:
+        json.dump({"horizon": horizon, "window": ws.WINDOW, "tolerance": ws.TOLERANCE, "judge": rows,
+                   "summary": summary}, f, indent=1)
+    # trailing-window means every 64 steps (the per-step series would be too large to keep)
+    series = {}
+    for i, r in enumerate(rows):
+        for tag, run in (("cold", cold), ("warm", warm)):
+            series[f"{tag}_cd_{r['seed']}"] = ws.trailing_mean(run["cd"][i])[63::64].astype(np.float32)
+            series[f"{tag}_cl_{r['seed']}"] = ws.trailing_mean(run["cl"][i])[63::64].astype(np.float32)
+    np.savez_compressed(os.path.join(args.out, "judge_window_means.npz"), **series)
+
+
+def single_lattice_step_s(dims, h, shape, steps=2048):
+    """Device seconds per LBM step of the plain path: one FP32 lattice through
+    wt_step (autotuned block shape, graphed step sequences)."""
+    import torch
+    from .engine import AeroEngine, ORIGIN_X, make_sim
+    from .workloads import CONFIG_SIM
+    e = AeroEngine(dims=dims, origin=(ORIGIN_X, 0.0, 0.0), h=h, sim=make_sim(**CONFIG_SIM))
+    try:
+        e.set_shape_raw(shape)
+        e.tune()
+        e.step(512)
+        st = torch.cuda.ExternalStream(e.stream())
+        a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(steps // 512):
+            e.step(512)
+        c.record(st)
+        c.synchronize()
+        return a.elapsed_time(c) / 1e3 / steps
+    finally:
+        e.close()
+
+
+def sweep_cases(small=False):
+    cases = aeromap_cases()
+    if small:
+        cases = cases[:3] + cases[25:27]
+    return [(d, h, shape) for d, _, h, shape, _ in cases], [lab for *_, lab in cases]
+
+
+def study_sweep(args):
+    """Time to 1 % convergence of all aero-map cases: plain FP32 cold start one case
+    after another (single-lattice launches) vs batched FP16 with the warm start."""
+    os.makedirs(args.out, exist_ok=True)
+    cases, labels = sweep_cases(args.small)
+    horizon = 4000 if args.small else args.judge_steps
+    model = load_model(args.weights)
+    log(f"{len(cases)} cases, horizon {horizon} steps")
+    # cold FP32 reference runs (batched for the study's own speed; the sequential
+    # cost of the plain path is its measured single-lattice step time x steps)
+    cold = ws.run_cases(cases, horizon, storage="f32")
+    refs = [ws.reference_values(cold["cd"][i], cold["cl"][i]) for i in range(len(cases))]
+    cold_steps = [ws.convergence_step(cold["cd"][i], cold["cl"][i], *refs[i]) for i in range(len(cases))]
+    # single-lattice FP32 step time of every case size (plain path: one lattice at a time)
+    t_single = {}
+    for d, h, sh in cases:
+        if d not in t_single:
+            t_single[d] = single_lattice_step_s(d, h, sh)
+    # warm start: inference, then all cases batched in FP16
+    t0 = time.time()
+    fields = warm_fields(model, [sh for _, _, sh in cases])
+    t_infer = time.time() - t0
+    warm = ws.run_cases(cases, horizon, warm=fields, storage="f16")
+    warm_steps = [ws.convergence_step(warm["cd"][i], warm["cl"][i], *refs[i]) for i in range(len(cases))]
+    # cold FP16 batched without the warm start (isolates the two effects)
+    coldb = ws.run_cases(cases, horizon, storage="f16")
+    coldb_steps = [ws.convergence_step(coldb["cd"][i], coldb["cl"][i], *refs[i]) for i in range(len(cases))]
+    H = horizon
+    plain_s = sum((c if c is not None else H) * t_single[d] for c, (d, _, _) in zip(cold_steps, cases))
+    batch_step = warm["group_step_s"][0]
+    warm_s = max((w if w is not None else H) for w in warm_steps) * batch_step + t_infer
+    coldb_s = max((w if w is not None else H) for w in coldb_steps) * coldb["group_step_s"][0]
+    res = {"cases": labels, "horizon": H, "cold_fp32_steps": cold_steps, "warm_fp16_batched_steps": warm_steps,
+           "cold_fp16_batched_steps": coldb_steps, "single_lattice_step_s": {str(k): v for k, v in t_single.items()},
+           "batched_fp16_step_s": batch_step, "inference_s": t_infer,
+           "plain_fp32_sequential_s": plain_s, "batched_fp16_cold_s": coldb_s, "batched_fp16_warm_s": warm_s,
+           "speedup_batched_warm": plain_s / warm_s, "speedup_batched_cold": plain_s / coldb_s,
+           "refs": refs}
+    log(json.dumps({k: v for k, v in res.items() if k not in ("cases", "refs")}))
+    with open(os.path.join(args.out, "sweep_study.json"), "w") as f:
+        json.dump(res, f, indent=1)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("study", choices=["warmstart", "judge", "sweep"])
+    ap.add_argument("--train-cases", type=int, default=400)
+    ap.add_argument("--val-cases", type=int, default=50)
+    ap.add_argument("--settle", type=int, default=24000)
+    ap.add_argument("--average", type=int, default=8000)
+    ap.add_argument("--out", default="gpurun_out/study")
+    ap.add_argument("--small", action="store_true")
+    ap.add_argument("--epochs", type=int, default=80)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--judge-steps", type=int, default=64000)
+    ap.add_argument("--weights", default=None)
+    args = ap.parse_args(argv)
+    import torch
+    torch.cuda.set_device(0)
+    {"warmstart": study_warmstart, "judge": study_judge, "sweep": study_sweep}[args.study](args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

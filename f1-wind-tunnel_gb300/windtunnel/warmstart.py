@@ -1,0 +1,249 @@
+"""Learned warm start of the aero-map cases and its judge.
+
+* Features: the car's signed distance sampled on the coarse 64x24x20 grid over
+  the tunnel (wt_sdf_sample), the front and rear ride heights, the three wing
+  angles of the reference F1 (front flap, rear main plane, rear flap; f1.ts:226,
+  261-262) and, as the fourth angle, the body's rake angle that the two ride
+  heights set (f1.ts:37-46); z is padded from 20 to 24 cells.
+* Targets: the fluid-cell box average of (ux, uy, uz, rho) of an FP32 LBM run of
+  the same case (wt_read_coarse), time-averaged after the flow has settled.
+* Use: the network's field goes through wt_reset_from (trilinear upsampling to
+  the lattice, equilibrium populations) in place of LBM_INIT's uniform state.
+* Judge: the LBM itself.  Cd and Cl of the whole car come from the per-step
+  FP64 force history; a run is converged at the first step after which the mean
+  over the trailing window (5760 steps, or all steps so far when fewer) stays
+  within 1 % of the reference value for both, the reference being the mean over
+  the last quarter of a long cold-start FP32 run of the same case.
+"""
+import math
+import time
+
+import numpy as np
+
+from . import _abi
+from .engine import AeroBatch, AeroEngine, DEG, ORIGIN_X, make_sim
+from .surrogate import COARSE, IN_CH, PADDED_Z
+from .workloads import CONFIG_SIM, config_f1_shape, drag_coefficient, half_area_cells, lift_coefficient
+
+WINDOW = 5760           # 12 s x 60 frames x 8 steps
+TOLERANCE = 0.01
+WHEELBASE_X = 3.4       # rake is referred to the wheelbase (f1.ts:37-46 rotates about the axle line)
+U_IN = CONFIG_SIM["u_in"]
+F1_DIMS, F1_H = (256, 96, 80), 0.045
+COARSE_H = F1_H * F1_DIMS[0] / COARSE[0]
+
+
+def coarse_grid():
+    g = _abi.Grid()
+    g.nx, g.ny, g.nz = COARSE
+    g.origin[0], g.origin[1], g.origin[2] = ORIGIN_X, 0.0, 0.0
+    g.h = COARSE_H
+    return g
+
+
+def case_shape(seed):
+    return config_f1_shape(seed)
+
+
+def scalars(shape):
+    rake = math.degrees(math.atan((shape.rear_ride - shape.ride_h) / WHEELBASE_X))
+    return np.array([(shape.ride_h - 0.035) / 0.025, (shape.rear_ride - 0.035) / 0.025,
+                     (shape.front_flap / DEG - 15.0) / 10.0, (shape.rear_main / DEG - 15.0) / 10.0,
+                     (shape.rear_flap / DEG - 15.0) / 10.0, rake / 0.5], np.float32)
+
+
+def features(shape, lib=None):
+    """Network input [PADDED_Z, 24, 64, 8] (float32) and loss mask [PADDED_Z, 24, 64]."""
+    import ctypes
+    lib = lib or _abi.load()
+    nx, ny, nz = COARSE
+    sdf = np.empty(nx * ny * nz, np.float32)
+    g = coarse_grid()
+    rc = lib.wt_sdf_sample(ctypes.byref(shape), ctypes.byref(g), sdf.ctypes.data)
+    if rc != 0:
+        raise _abi.WindTunnelError(rc, "wt_sdf_sample: " + lib.wt_last_error(None).decode())
+    sdf = sdf.reshape(nz, ny, nx)
+    x = np.zeros((PADDED_Z, ny, nx, IN_CH), np.float32)
+    x[:, :, :, 0] = 1.0
+    x[:nz, :, :, 0] = np.tanh(sdf / 0.3)
+    x[:, :, :, 1:7] = scalars(shape)
+    mask = np.zeros((PADDED_Z, ny, nx), np.float32)
+    mask[:nz] = (sdf > 0.0).astype(np.float32)
+    return x, mask
+
+
+def normalize_target(coarse):
+    """[20, 24, 64, 4] (ux, uy, uz, rho) -> normalised [24, 24, 64, 4]."""
+    t = np.zeros((PADDED_Z,) + coarse.shape[1:], np.float32)
+    nz = coarse.shape[0]
+    t[:nz, ..., 0] = coarse[..., 0] / U_IN - 1.0
+    t[:nz, ..., 1] = coarse[..., 1] / U_IN
+    t[:nz, ..., 2] = coarse[..., 2] / U_IN
+    t[:nz, ..., 3] = (coarse[..., 3] - 1.0) * 100.0
+    return t
+
+
+def denormalize(pred):
+    """Network output [24, 24, 64, >=4] -> coarse field [20, 24, 64, 4] for wt_reset_from."""
+    p = np.asarray(pred, np.float32)[: COARSE[2], ..., :4]
+    out = np.empty(p.shape, np.float32)
+    out[..., 0] = (p[..., 0] + 1.0) * U_IN
+    out[..., 1] = p[..., 1] * U_IN
+    out[..., 2] = p[..., 2] * U_IN
+    out[..., 3] = 1.0 + p[..., 3] / 100.0
+    return out
+
+
+# --------------------------------------------------------------------------- LBM runs
+def coefficient_series(hist9, area):
+    fx = hist9[:, 0] + hist9[:, 3] + hist9[:, 6]
+    fy = hist9[:, 1] + hist9[:, 4] + hist9[:, 7]
+    return drag_coefficient(fx, U_IN, area), lift_coefficient(fy, U_IN, area)
+
+
+def run_cases(cases, steps, chunk=2048, warm=None, storage="f32", average=None, group=64, tune=True, log=None):
+    """Advance every case (list of (dims, h, shape)) from a cold or warm start for
+    `steps` steps in batched launches.  warm: list of coarse fields (or None).
+    average: (first_step, every) -> also return the time average of the coarse
+    field sampled every `every` steps from `first_step` on.
+    Returns dict with per-case 'cd', 'cl' (per step), 'area', optional 'coarse',
+    and the measured device seconds per LBM step of each group."""
+    sim = make_sim(storage=storage, **CONFIG_SIM)
+    out = {"cd": [], "cl": [], "area": [], "coarse": [], "group_step_s": [], "group_cells": []}
+    for g0 in range(0, len(cases), group):
+        part = cases[g0:g0 + group]
+        b = AeroBatch([(d, (ORIGIN_X, 0.0, 0.0), h) for d, h, _ in part], sim)
+        try:
+            areas = []
+            for k, (d, h, shape) in enumerate(part):
+                e = b.lattices[k]
+                e.set_shape_raw(shape)
+                if warm is not None and warm[g0 + k] is not None:
+                    e.reset_from(warm[g0 + k])
+                areas.append(half_area_cells(e.debug_read()["solid"], d))
+            if tune:
+                b.tune()
+            hist = [[] for _ in part]
+            acc = [None] * len(part)
+            nacc = 0
+            done, t_dev = 0, 0.0
+            import torch
+            st = torch.cuda.ExternalStream(b.stream())
+            step_chunk = average[1] if average is not None else chunk
+            assert step_chunk % 2 == 0 and steps % 2 == 0
+            while done < steps:
+                n = min(step_chunk, steps - done)
+                a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(st)
+                b.step(n)
+                c.record(st)
+                c.synchronize()
+                t_dev += a.elapsed_time(c) / 1e3
+                done += n
+                for k, (d, h, shape) in enumerate(part):
+                    hist[k].append(b.lattices[k].force_history(n))
+                if average is not None and done > average[0]:
+                    for k, (d, h, shape) in enumerate(part):
+                        f = b.lattices[k].read_coarse(*COARSE).astype(np.float64)
+                        acc[k] = f if acc[k] is None else acc[k] + f
+                    nacc += 1
+                if log:
+                    log(f"cases {g0}-{g0 + len(part) - 1}: {done}/{steps} steps")
+            out["group_step_s"].append(t_dev / max(1, done))
+            out["group_cells"].append(int(sum(int(np.prod(d)) for d, _, _ in part)))
+            for k in range(len(part)):
+                h9 = np.concatenate(hist[k])
+                cd, cl = coefficient_series(h9, areas[k])
+                out["cd"].append(cd)
+                out["cl"].append(cl)
+                out["area"].append(areas[k])
+                if average is not None:
+                    out["coarse"].append((acc[k] / max(1, nacc)).astype(np.float32))
+        finally:
+            b.close()
+    return out
+
+
+def trailing_mean(x, window=WINDOW):
+    c = np.concatenate([[0.0], np.cumsum(np.asarray(x, np.float64))])
+    t = np.arange(1, len(x) + 1)
+    lo = np.maximum(0, t - window)
+    return (c[t] - c[lo]) / (t - lo)
+
+
+def convergence_step(cd, cl, ref_cd, ref_cl, window=WINDOW, tol=TOLERANCE):
+    """First step (1-based count) after which both trailing means stay within tol of
+    the reference values until the end of the series; None if the last step is not."""
+    ok = (np.abs(trailing_mean(cd, window) - ref_cd) <= tol * abs(ref_cd)) & \
+         (np.abs(trailing_mean(cl, window) - ref_cl) <= tol * abs(ref_cl))
+    if not ok[-1]:
+        return None
+    bad = np.nonzero(~ok)[0]
+    return int(bad[-1] + 2) if len(bad) else 1
+
+
+def reference_values(cd, cl):
+    """Long-run values: mean over the last quarter of the series (the lift of these
+    cases still creeps on the viscous time scale late into a run)."""
+    h = (3 * len(cd)) // 4
+    return float(np.mean(cd[h:])), float(np.mean(cl[h:]))
+
+
+def convergence_step_cd(cd, ref_cd, window=WINDOW, tol=TOLERANCE):
+    """As convergence_step, drag only."""
+    ok = np.abs(trailing_mean(cd, window) - ref_cd) <= tol * abs(ref_cd)
+    if not ok[-1]:
+        return None
+    bad = np.nonzero(~ok)[0]
+    return int(bad[-1] + 2) if len(bad) else 1
+
+
+# --------------------------------------------------------------------------- training
+def train(model, X, T, M, epochs=60, batch=16, lr=2e-3, seed=0, log=None):
+    """X [n, 24, 24, 64, 8] (float32 numpy), T [n, 24, 24, 64, 4], M [n, 24, 24, 64]."""
+    import torch
+    rng = np.random.default_rng(seed)
+    n = len(X)
+    Xd = torch.tensor(X, device="cuda").to(torch.bfloat16)
+    Td = torch.tensor(T, device="cuda")
+    Md = torch.tensor(M, device="cuda")
+    steps_per_epoch = max(1, n // batch)
+    total = epochs * steps_per_epoch
+    history = []
+    t0 = time.time()
+    k = 0
+    for ep in range(epochs):
+        perm = torch.tensor(rng.permutation(n), device="cuda")
+        ep_loss, ep_norm = 0.0, 0.0
+        losses = []
+        for s in range(steps_per_epoch):
+            idx = perm[s * batch:(s + 1) * batch]
+            cur_lr = lr * 0.5 * (1.0 + math.cos(math.pi * k / total))  # cosine decay
+            loss, norm = model.train_step(Xd[idx].contiguous(), Td[idx].contiguous(), Md[idx].contiguous(), cur_lr)
+            losses.append((loss, norm))
+            k += 1
+        torch.cuda.synchronize()
+        model.ops.check()
+        ep_loss = sum(float(l) for l, _ in losses)
+        ep_norm = sum(nm for _, nm in losses)
+        history.append(ep_loss / ep_norm)
+        if log:
+            log(f"epoch {ep + 1}/{epochs}: loss {history[-1]:.5f} ({time.time() - t0:.1f} s)")
+    return history
+
+
+def predict(model, X, batch=16):
+    import torch
+    out = []
+    for i in range(0, len(X), batch):
+        x = torch.tensor(X[i:i + batch], device="cuda").to(torch.bfloat16)
+        y = model.forward(x)
+        out.append(y.float().cpu().numpy())
+    model.ops.check()
+    return np.concatenate(out)
+
+
+def validation_loss(model, X, T, M, batch=16):
+    P = predict(model, X, batch)
+    e = (P[..., :4] - T) ** 2 * M[..., None]
+    return float(e.sum() / max(1.0, 4.0 * M.sum()))
