@@ -219,13 +219,75 @@ def run_aeromap(args, rank, world, dist):
     b.close()
 
 
+def surrogate_flops(batch, d, h, w):
+    """Multiply-add FLOPs (2 per MAC) of one training step's convolutions: forward,
+    data gradient (not for the first layer) and weight gradient of every layer."""
+    from windtunnel.surrogate import Surrogate
+    level = {"e0": 0, "e1": 1, "e2": 2, "e3": 3, "d2": 2, "d1": 1, "d0": 0, "he": 0}
+    total = 0
+    for name, cin, cout, taps, _ in Surrogate.LAYERS:
+        lv = level[name[:2]]
+        vox = batch * (d >> lv) * (h >> lv) * (w >> lv)
+        mac = vox * cout * cin * taps
+        total += 2 * mac * (2 if name == "e0a" else 3)
+    return total
+
+
+def run_surrogate(args, rank, world):
+    """Training steps of the warm-start network (tensor-core convolutions) on
+    synthetic inputs of the network's shape: samples/s and conv TFLOP/s."""
+    import numpy as np
+    import torch
+    from windtunnel.surrogate import Surrogate
+    B, D, H, W = 16, 24, 24, 64
+    rng = np.random.default_rng(args.seed)
+    model = Surrogate(seed=args.seed)
+    x = torch.tensor(rng.standard_normal((B, D, H, W, 8)).astype(np.float32) * 0.5, device="cuda").to(torch.bfloat16)
+    t = torch.tensor(rng.standard_normal((B, D, H, W, 4)).astype(np.float32) * 0.1, device="cuda")
+    m = torch.ones((B, D, H, W), dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        model.train_step(x, t, m, 1e-4)
+    torch.cuda.synchronize()
+    model.ops.check()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            model.train_step(x, t, m, 1e-4)
+        e1.record(st)
+        torch.cuda.synchronize()
+    model.ops.check()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = surrogate_flops(B, D, H, W)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, kind = float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak, kind = 1900.0, "fallback"
+    tf = flops / (ms / 1e3) / 1e12
+    clocks = clk.summary()
+    line = {"metric": "samples/s", "value": B / (ms / 1e3), "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "warm-start network training step (forward, backward, Adam), batch 16 at "
+                                   "64x24x24 with 8 input channels, 15 convolution layers",
+                       "conv_flops_per_step": flops},
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+                         "traffic": None, "peak_source": kind,
+                         "note": "convolution FLOPs over the whole step time (element-wise kernels included)"},
+            "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200, help="timed frames")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="wt", choices=["wt", "reference"])
-    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap"])
+    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "surrogate"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-frames", type=int, default=4)
@@ -264,6 +326,11 @@ def main():
     torch.cuda.init()
     import windtunnel
     from windtunnel.workloads import bytes_per_lup
+    if args.workload == "surrogate":
+        run_surrogate(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
     if args.workload == "aeromap":
         run_aeromap(args, rank, world, dist)
         if dist:
