@@ -98,84 +98,109 @@ __device__ __forceinline__ int tap_dz(uint32_t t, uint32_t taps) { return taps =
 __device__ __forceinline__ int tap_dy(uint32_t t, uint32_t taps) { return taps == 27 ? (int)((t / 3) % 3) - 1 : 0; }
 __device__ __forceinline__ int tap_dx(uint32_t t, uint32_t taps) { return taps == 27 ? (int)(t % 3) - 1 : 0; }
 
-// Voxel m shifted by (sz, sy, sx) inside the same batch item, or -1 outside the grid.
-__device__ __forceinline__ int64_t shifted(const GemmArgs& p, uint32_t m, int sz, int sy, int sx) {
-  const uint32_t x = m % p.w, y = (m / p.w) % p.h, z = (m / (p.w * p.h)) % p.d, bi = m / (p.w * p.h * p.d);
-  const int xx = (int)x + sx, yy = (int)y + sy, zz = (int)z + sz;
-  if (xx < 0 || yy < 0 || zz < 0 || xx >= (int)p.w || yy >= (int)p.h || zz >= (int)p.d) return -1;
-  return (((int64_t)bi * p.d + zz) * p.h + yy) * p.w + xx;
-}
-
 // Byte offset of 16-byte chunk (row r, k-group g) in the core-matrix layout.
 __device__ __forceinline__ uint32_t chunk_off(uint32_t r, uint32_t g) { return ((r >> 3) * 8u + g) * 128u + (r & 7u) * 16u; }
 
 __device__ __forceinline__ uint4 ld16(const __nv_bfloat16* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
 
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+
+// Grid position of a voxel (x fastest, then y, z, batch item).
+struct VoxPos {
+  int x, y, z;
+  int64_t vox;
+  bool ok;
+};
+
+__device__ __forceinline__ VoxPos vox_pos(const GemmArgs& p, uint32_t m, uint32_t end) {
+  VoxPos r;
+  r.ok = m < end;
+  const uint32_t mm = r.ok ? m : 0u;
+  r.x = (int)(mm % p.w);
+  r.y = (int)((mm / p.w) % p.h);
+  r.z = (int)((mm / (p.w * p.h)) % p.d);
+  r.vox = mm;
+  return r;
 }
 
-// Gather K slice kt (k in [k0, k0 + 64)) of both operands into stage buffers sa, sb.
+// Index of the voxel r + (dz, dy, dx) in the same batch item, or -1 outside the grid.
+__device__ __forceinline__ int64_t nbr(const GemmArgs& p, const VoxPos& r, int dz, int dy, int dx) {
+  const int xx = r.x + dx, yy = r.y + dy, zz = r.z + dz;
+  if ((unsigned)xx >= p.w || (unsigned)yy >= p.h || (unsigned)zz >= p.d) return -1;
+  return r.vox + ((int64_t)dz * p.h + dy) * p.w + dx;
+}
+
+// Gather K slice [k0, k0 + 64) of both operands into the stage buffers sa, sb.
+//   FWD / DGRAD: thread t owns A row t (a voxel, position precomputed in `row`)
+//   and B row t (a weight row); each 16-byte chunk is 8 consecutive channels of
+//   one tap, one vector load.
+//   WGRAD: K runs over voxels; thread t owns voxel k0 + (t & 63) and half
+//   (t >> 6) of the A rows (taps x channels) and B rows (output channels); it
+//   loads 8 channels of its voxel with one vector load and stores them into 8
+//   rows of the K-major tile (2-byte stores).
+// Rows past the MMA's N (B) are never read and not written; K past the range
+// is zero in both operands.
 template <int MODE>
-__device__ __forceinline__ void gather(const GemmArgs& p, uint32_t tile_m, uint32_t k0, uint32_t k_end, uint8_t* sa,
-                                       uint8_t* sb) {
+__device__ __forceinline__ void gather(const GemmArgs& p, const VoxPos& row, uint32_t tile_m, uint32_t n_mma,
+                                       uint32_t k0, uint32_t k_end, uint8_t* sa, uint8_t* sb) {
   const uint32_t t = threadIdx.x;
-  // ---- A: row t of the tile, 8 k-groups
-  {
-    const uint32_t row = tile_m + t;
-#pragma unroll 1
+  if constexpr (MODE == FWD || MODE == DGRAD) {
+    const uint32_t C = (MODE == FWD) ? p.cin : p.cout;
+    const int sg = (MODE == FWD) ? 1 : -1;
+    uint32_t tap = k0 / C, c = k0 % C;
+#pragma unroll
     for (uint32_t g = 0; g < 8; g++) {
       const uint32_t k = k0 + 8 * g;
       uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (row < p.M && k < k_end) {
-        if constexpr (MODE == FWD) {
-          const uint32_t tap = k / p.cin, ci = k % p.cin;
-          const int64_t s = shifted(p, row, tap_dz(tap, p.taps), tap_dy(tap, p.taps), tap_dx(tap, p.taps));
-          if (s >= 0) v = ld16(p.a + (size_t)s * p.cin + ci);
-        } else if constexpr (MODE == DGRAD) {
-          const uint32_t tap = k / p.cout, co = k % p.cout;
-          const int64_t s = shifted(p, row, -tap_dz(tap, p.taps), -tap_dy(tap, p.taps), -tap_dx(tap, p.taps));
-          if (s >= 0) v = ld16(p.a + (size_t)s * p.cout + co);
-        } else {  // WGRAD: row = (tap, ci), k = voxel
-          const uint32_t tap = row / p.cin, ci = row % p.cin;
-          const int dz = tap_dz(tap, p.taps), dy = tap_dy(tap, p.taps), dx = tap_dx(tap, p.taps);
-          __nv_bfloat16 e[8];
-#pragma unroll
-          for (int j = 0; j < 8; j++) {
-            e[j] = __float2bfloat16_rn(0.0f);
-            const uint32_t m = k + j;
-            if (m < k_end) {
-              const int64_t s = shifted(p, m, dz, dy, dx);
-              if (s >= 0) e[j] = p.a[(size_t)s * p.cin + ci];
-            }
-          }
-          v = make_uint4(pack2(e[0], e[1]), pack2(e[2], e[3]), pack2(e[4], e[5]), pack2(e[6], e[7]));
-        }
+      if (row.ok && k < k_end) {
+        const int64_t sv = nbr(p, row, sg * tap_dz(tap, p.taps), sg * tap_dy(tap, p.taps), sg * tap_dx(tap, p.taps));
+        if (sv >= 0) v = ld16(p.a + (size_t)sv * C + c);
       }
       *reinterpret_cast<uint4*>(sa + chunk_off(t, g)) = v;
-    }
-  }
-  // ---- B: row t (< 128) of the tile, rows >= N zero
-  {
-    const uint32_t row = t;
-#pragma unroll 1
-    for (uint32_t g = 0; g < 8; g++) {
-      const uint32_t k = k0 + 8 * g;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (row < p.N && k < k_end) {
-        if constexpr (MODE == FWD || MODE == DGRAD) {
-          v = ld16(p.b + (size_t)row * p.K + k);
-        } else {  // WGRAD: B[co][m] = dy[m][co]
-          __nv_bfloat16 e[8];
-#pragma unroll
-          for (int j = 0; j < 8; j++) {
-            const uint32_t m = k + j;
-            e[j] = (m < k_end) ? p.b[(size_t)m * p.cout + row] : __float2bfloat16_rn(0.0f);
-          }
-          v = make_uint4(pack2(e[0], e[1]), pack2(e[2], e[3]), pack2(e[4], e[5]), pack2(e[6], e[7]));
-        }
+      c += 8;
+      if (c >= C) {
+        c = 0;
+        tap++;
       }
-      *reinterpret_cast<uint4*>(sb + chunk_off(row, g)) = v;
+    }
+    if (t < n_mma) {
+#pragma unroll
+      for (uint32_t g = 0; g < 8; g++) {
+        const uint32_t k = k0 + 8 * g;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (t < p.N && k < k_end) v = ld16(p.b + (size_t)t * p.K + k);
+        *reinterpret_cast<uint4*>(sb + chunk_off(t, g)) = v;
+      }
+    }
+  } else {
+    const uint32_t j = t & 63u, half = t >> 6;
+    const VoxPos m = vox_pos(p, k0 + j, k_end);
+    const uint32_t jo = (j & 7u) * 2u, jg = j >> 3;
+    // A rows half*64 .. +63 = (tap, ci) rows tile_m + ...
+#pragma unroll
+    for (uint32_t q = 0; q < 8; q++) {
+      const uint32_t r0 = half * 64u + 8u * q, R0 = tile_m + r0;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (m.ok && R0 < p.M) {
+        const uint32_t tap = R0 / p.cin, ci = R0 % p.cin;
+        const int64_t sv = nbr(p, m, tap_dz(tap, p.taps), tap_dy(tap, p.taps), tap_dx(tap, p.taps));
+        if (sv >= 0) v = ld16(p.a + (size_t)sv * p.cin + ci);
+      }
+      const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int e = 0; e < 8; e++)
+        *reinterpret_cast<uint16_t*>(sa + chunk_off(r0 + e, jg) + jo) = (uint16_t)(w4[e >> 1] >> ((e & 1) * 16));
+    }
+    // B rows (output channels) half*64 .. +63, only those the MMA reads
+#pragma unroll
+    for (uint32_t q = 0; q < 8; q++) {
+      const uint32_t r0 = half * 64u + 8u * q;
+      if (r0 >= n_mma) break;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (m.ok && r0 < p.N) v = ld16(p.b + (size_t)m.vox * p.cout + r0);
+      const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int e = 0; e < 8; e++)
+        *reinterpret_cast<uint16_t*>(sb + chunk_off(r0 + e, jg) + jo) = (uint16_t)(w4[e >> 1] >> ((e & 1) * 16));
     }
   }
 }
@@ -183,8 +208,7 @@ __device__ __forceinline__ void gather(const GemmArgs& p, uint32_t tile_m, uint3
 template <int MODE>
 __global__ void __launch_bounds__(NTHREADS, 1) conv_gemm_kernel(GemmArgs p) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sA[2] = {smem, smem + STAGE_BYTES};
-  uint8_t* sB[2] = {smem + 2 * STAGE_BYTES, smem + 3 * STAGE_BYTES};
+  // stage s: A at smem + s * STAGE_BYTES, B at smem + (2 + s) * STAGE_BYTES
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 4 * STAGE_BYTES);  // [2]
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 4 * STAGE_BYTES + 16);
   const uint32_t t = threadIdx.x, warp = t >> 5;
@@ -211,6 +235,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) conv_gemm_kernel(GemmArgs p) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
+  const VoxPos row_pos = vox_pos(p, tile_m + t, p.M);  // FWD / DGRAD: this thread's A row (a voxel)
   bool ok = true;
   uint32_t issued = 0;  // K slices whose MMAs were issued (uniform across the block)
   for (uint32_t kt = 0; kt < nk; kt++) {
@@ -221,12 +246,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) conv_gemm_kernel(GemmArgs p) {
       ok = false;
       break;
     }
-    gather<MODE>(p, tile_m, k_begin + kt * BK, k_end, sA[s], sB[s]);
+    uint8_t* const sa = smem + s * STAGE_BYTES;
+    uint8_t* const sb = smem + (2u + s) * STAGE_BYTES;
+    gather<MODE>(p, row_pos, tile_m, n_mma, k_begin + kt * BK, k_end, sa, sb);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (t == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a0 = smem_u32(sA[s]), b0 = smem_u32(sB[s]);
+      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
 #pragma unroll
       for (uint32_t kk = 0; kk < BK / 16; kk++) {
         const uint64_t ad = smem_desc(a0 + kk * 256u, 128u, 1024u);

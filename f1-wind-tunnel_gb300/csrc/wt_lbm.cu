@@ -226,16 +226,31 @@ __device__ __forceinline__ void link_force(float v, uint32_t group, float (&gf)[
 // ---------------------------------------------------------------------------
 constexpr uint32_t TILE = 128;
 
-// Slot offsets of direction i relative to the cell index (mod 2^32), read from
-// the host-computed tables of the lattice's arguments (the kernel parameter
-// block, or the batch kernel's shared-memory copy).
+// Slot offsets of direction i relative to the cell index (mod 2^32): the
+// single-lattice kernel reads the host-computed tables straight from its
+// parameter block and takes the plain-neighbour path and the L2 prefetch; the
+// batch kernel, whose arguments sit in global memory, computes own-slot
+// addresses from np and keeps the two-way (interior / face) gather.  (Staging
+// the batch arguments in shared memory to give it the plain path measured 8-10 %
+// slower on the 33-lattice aero map; reading 57 table entries from global
+// memory instead spills ~400 B per thread.)
 struct OfsTable {
+  static constexpr bool plain_path = true;
   const StepArgs& a;
   template <int i, class PT> __device__ __forceinline__ PT* own_at(PT* P, uint32_t idx) const {
     return P + (idx + a.own_ofs[i]);
   }
   template <int i> __device__ __forceinline__ uint32_t pull() const { return a.pull_ofs[i]; }
   template <int i> __device__ __forceinline__ uint32_t push() const { return a.push_ofs[i]; }
+};
+struct OfsCalc {
+  static constexpr bool plain_path = false;
+  uint32_t np;
+  template <int i, class PT> __device__ __forceinline__ PT* own_at(PT* P, uint32_t idx) const {
+    return P + (size_t)i * np + idx;
+  }
+  template <int i> __device__ __forceinline__ uint32_t pull() const { return 0u; }
+  template <int i> __device__ __forceinline__ uint32_t push() const { return 0u; }
 };
 
 // L2 prefetch of the tile a.prefetch_ahead blocks further on (about one wave of
@@ -277,7 +292,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
   const bool in = (x < nx) && (y < ny);
   const uint32_t nxy = nx * ny;
   const uint32_t np = (uint32_t)a.np;
-  prefetch_tile<typename St::T>(a, bid, gdim);
+  if constexpr (Ofs::plain_path) prefetch_tile<typename St::T>(a, bid, gdim);
   const uint32_t idx = in ? x + nx * y + nxy * z : 0u;
   const uint32_t cw = in ? __ldg(a.cellw + idx) : CW_SOLID;
   typedef typename St::T PT;
@@ -297,12 +312,13 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
   // Warp-uniform plain test (all lanes converged here): no fluid lane of this
   // warp has a bounce-back link, so every population moves between plain
   // neighbour slots.
-  const bool plain =
+  const bool plain = Ofs::plain_path &&
       __all_sync(0xffffffffu, !in || (cw & CW_SOLID) || (!yzface && (cw & CW_LINKS) == 0u));
 
   if (in && (cw & CW_SOLID)) {
     if constexpr (!GATHER) {  // wgsl.ts:183: solid cells hold w_i
-      sfor<19>([&](auto K) { St::st(ofs.template own_at<K>(P, idx), Wd(K), Wd(K)); });
+      if constexpr (Ofs::plain_path) sfor<19>([&](auto K) { St::st(ofs.template own_at<K>(P, idx), Wd(K), Wd(K)); });
+      else sfor<19>([&](auto K) { stp<St>(a.pop, K, np, idx, Wd(K), K); });
     }
     if constexpr (FIELDS) a.fields[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
   } else if (in) {
@@ -415,7 +431,8 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
     if constexpr (!GATHER) {
       sfor<19>([&](auto J) {
         constexpr int j = J;
-        St::st(ofs.template own_at<OPPd(j)>(P, idx), fo[j], Wd(j));
+        if constexpr (Ofs::plain_path) St::st(ofs.template own_at<OPPd(j)>(P, idx), fo[j], Wd(j));
+        else stp<St>(a.pop, OPPd(j), np, idx, fo[j], j);
       });
     } else if (plain) {
       sfor<19>([&](auto J) {
@@ -575,18 +592,9 @@ __global__ void __launch_bounds__(256, 4) batch_step_kernel(const StepArgs* __re
   const uint32_t t = b - tl.base;
   const uint3 gdim = make_uint3(tl.gx, tl.gy, tl.gz);
   const uint3 bid = make_uint3(t % tl.gx, (t / tl.gx) % tl.gy, t / (tl.gx * tl.gy));
-  // The lattice's arguments are staged in shared memory: the step body then reads
-  // its slot-offset tables and constants there instead of holding them in
-  // registers (which spilled when they were read from global memory).
-  __shared__ StepArgs sa;
-  {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(&args[lo]);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(&sa);
-    for (uint32_t i = threadIdx.x + blockDim.x * threadIdx.y; i < sizeof(StepArgs) / 4; i += blockDim.x * blockDim.y)
-      dst[i] = src[i];
-  }
-  __syncthreads();
-  step_tile<St, GATHER, FIELDS>(sa, OfsTable{sa}, sa.slots + (size_t)pending * sa.nslots, bid, gdim);
+  const StepArgs& a = args[lo];
+  const OfsCalc ofs{(uint32_t)a.np};
+  step_tile<St, GATHER, FIELDS>(a, ofs, a.slots + (size_t)pending * a.nslots, bid, gdim);
 }
 
 // Canonical initial state (LBM_INIT, wgsl.ts:147-155): f*_j = feq_j(1, (u_in,0,0))
