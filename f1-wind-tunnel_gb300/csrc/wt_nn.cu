@@ -123,21 +123,36 @@ __global__ void grad_to_bf16_kernel(const float* __restrict__ g, const float* __
   }
 }
 
-// One block per channel group of 32 channels x 8 row-phases; fixed summation order.
-__global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ dy, float* __restrict__ db, uint64_t rows,
-                                 uint32_t c) {
-  const uint32_t ch = blockIdx.x * 32 + (threadIdx.x & 31), ph = threadIdx.x >> 5;  // 8 phases
-  __shared__ float part[8][32];
-  float s = 0.0f;
-  if (ch < c)
-    for (uint64_t r = ph; r < rows; r += 8) s += __bfloat162float(dy[r * c + ch]);
-  part[ph][threadIdx.x & 31] = s;
+// Bias gradient in two passes with a fixed summation order: block b of the first
+// pass sums rows [b * chunk, (b + 1) * chunk) of every channel (thread t owns
+// channel t % c and every (TB / c)-th row of the chunk, then the block folds its
+// row phases in order) into partial[b][c]; the second pass sums the blocks.
+constexpr uint32_t BG_BLOCKS = 512;
+
+__global__ void bias_grad_partial_kernel(const __nv_bfloat16* __restrict__ dy, float* __restrict__ partial,
+                                         uint64_t rows, uint32_t c, uint64_t chunk) {
+  __shared__ float red[TB];
+  const uint32_t phases = TB / c;  // c divides TB (c in {8, 16, 32, 64, 128})
+  const uint32_t ch = threadIdx.x % c, ph = threadIdx.x / c;
+  const uint64_t r0 = (uint64_t)blockIdx.x * chunk, r1 = min(rows, r0 + chunk);
+  float acc = 0.0f;
+  for (uint64_t r = r0 + ph; r < r1; r += phases) acc += __bfloat162float(dy[r * c + ch]);
+  red[threadIdx.x] = acc;
   __syncthreads();
-  if (ph == 0 && ch < c) {
+  if (threadIdx.x < c) {
     float t = 0.0f;
-    for (int q = 0; q < 8; q++) t += part[q][threadIdx.x & 31];
-    db[ch] = t;
+    for (uint32_t q = 0; q < phases; q++) t += red[q * c + threadIdx.x];
+    partial[(size_t)blockIdx.x * c + threadIdx.x] = t;
   }
+}
+
+__global__ void bias_grad_final_kernel(const float* __restrict__ partial, float* __restrict__ db, uint32_t nblocks,
+                                       uint32_t c) {
+  const uint32_t ch = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ch >= c) return;
+  float t = 0.0f;
+  for (uint32_t b = 0; b < nblocks; b++) t += partial[(size_t)b * c + ch];
+  db[ch] = t;
 }
 
 // Per-block partial loss in double (fixed order), gradient written per element.
@@ -278,8 +293,14 @@ int wt_nn_grad_to_bf16(const float* g, const float* g2, const void* act, void* o
 }
 
 int wt_nn_bias_grad(const void* dy, float* db, uint64_t rows, uint32_t c, void* stream) {
-  if (!dy || !db || !c) return bad("wt_nn_bias_grad");
-  bias_grad_kernel<<<(c + 31) / 32, 256, 0, S(stream)>>>(static_cast<const bf*>(dy), db, rows, c);
+  if (!dy || !db || !c || c > TB || TB % c) return bad("wt_nn_bias_grad");
+  static float* partial = nullptr;  // BG_BLOCKS x 256 floats, allocated once
+  if (!partial && cudaMalloc(&partial, (size_t)BG_BLOCKS * TB * sizeof(float)) != cudaSuccess)
+    return bad("wt_nn_bias_grad scratch");
+  const uint64_t chunk = rows ? (rows + BG_BLOCKS - 1) / BG_BLOCKS : 1;
+  const uint32_t nb = (uint32_t)(rows ? (rows + chunk - 1) / chunk : 1);
+  bias_grad_partial_kernel<<<nb, TB, 0, S(stream)>>>(static_cast<const bf*>(dy), partial, rows, c, chunk);
+  bias_grad_final_kernel<<<(c + 127) / 128, 128, 0, S(stream)>>>(partial, db, nb, c);
   return done("wt_nn_bias_grad");
 }
 

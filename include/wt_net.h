@@ -60,7 +60,8 @@ int wt_nn_up2_backward(const float* dy, float* dx, uint32_t batch, uint32_t d, u
 int wt_nn_add(const void* a, const void* b, void* y, uint64_t n, void* stream);
 /* out = bf16((g + g2) * (act > 0)); g2 and act may be NULL (no term / no mask). */
 int wt_nn_grad_to_bf16(const float* g, const float* g2, const void* act, void* out, uint64_t n, void* stream);
-/* db[c] = sum over rows of dy[rows][c] (FP32, overwritten). */
+/* db[c] = sum over rows of dy[rows][c] (FP32, overwritten, fixed summation
+ * order); c must divide 256. */
 int wt_nn_bias_grad(const void* dy, float* db, uint64_t rows, uint32_t c, void* stream);
 /* Masked mean-square error of pred[m][0:4] (BF16, row stride cp) against
  * target[m][0:4] (FP32): loss_sum[0] += sum mask*(p-t)^2; dpred[m][k] =
