@@ -190,6 +190,8 @@ static inline f32 dot(const vec3f& a, const vec3f& b) { return a.x * b.x + a.y *
 static inline f32 dot(const vec4f& a, const vec4f& b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
 static inline f32 length(f32 x) { return abs(x); }
 template <class V> static inline f32 length(const V& v) { return sqrt(dot(v, v)); }
+// normalize(e) = e / length(e), one IEEE division per component
+template <class V> static inline V normalize(const V& v) { return v / length(v); }
 
 template <class T> static inline T bitcast(f32 x) { T r; memcpy(&r, &x, 4); return r; }
 
@@ -206,6 +208,6 @@ template <class T> static inline T atomicLoad(T* p) { return __atomic_load_n(p, 
   using rt::vec2u; using rt::vec3u; using rt::vec4u; using rt::texture3d; using rt::sampler;         \
   using rt::to_f32; using rt::to_i32; using rt::to_u32; using rt::abs; using rt::min; using rt::max; \
   using rt::clamp; using rt::mix; using rt::smoothstep; using rt::select; using rt::sqrt;            \
-  using rt::floor; using rt::round; using rt::sign; using rt::sin; using rt::cos; using rt::atan;    \
+  using rt::floor; using rt::normalize; using rt::round; using rt::sign; using rt::sin; using rt::cos; using rt::atan;    \
   using rt::dot; using rt::length; using rt::bitcast; using rt::atomicAdd; using rt::atomicStore;   \
   using rt::atomicLoad; using rt::textureSampleLevel; using rt::textureDimensions;

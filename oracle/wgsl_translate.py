@@ -199,6 +199,9 @@ def cxx_type(t):
     m = re.match(r"atomic<(.*)>$", t)
     if m:
         return f"atomic<{cxx_type(m.group(1))}>"
+    m = re.match(r"ptr<\s*function\s*,\s*(.*)>$", t)
+    if m:
+        return f"{cxx_type(m.group(1))}*"
     if t == "texture_3d<f32>":
         return "texture3d"
     return t
@@ -371,7 +374,7 @@ def stmt_rewrite(s):
 def main():
     eng = os.path.join(REF, "src", "engine")
     table = {}
-    for f in ("wgsl.ts", "f1.ts", "car-model.ts"):
+    for f in ("wgsl.ts", "f1.ts", "car-model.ts", "render-wgsl.ts"):
         table.update(extract_consts(os.path.join(eng, f)))
     rig = rig_constants(os.path.join(eng, "car-model.ts"))
     report = []
@@ -380,6 +383,8 @@ def main():
         "m_lbm_step": "LBM_STEP",
         "m_voxelize": "VOXELIZE",
         "m_heat": "HEAT",
+        "m_particles": "PARTICLES_SIM",
+        "m_stream": "STREAM_SIM",
     }
     os.makedirs(OUT, exist_ok=True)
     chunks = [
