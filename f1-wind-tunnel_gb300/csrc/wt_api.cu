@@ -12,6 +12,7 @@
 
 #include "wt_fmath.h"
 #include "wt_internal.h"
+#include "wt_fields.h"
 #include "wt_lattice.cuh"
 
 using namespace wt;
@@ -688,6 +689,97 @@ int wt_sdf_sample(const wt_shape* shape, const wt_grid* grid, float* out) {
   if (e == cudaSuccess) e = cudaMemcpy(out, tmp, bytes, cudaMemcpyDeviceToHost);
   if (tmp) cudaFree(tmp);
   if (e != cudaSuccess) return fail(nullptr, WT_ERR_CUDA, std::string("wt_sdf_sample: ") + cudaGetErrorString(e));
+  return WT_OK;
+}
+
+namespace {
+FieldGrid field_grid(const wt_ctx* c) {
+  FieldGrid g;
+  g.nx = c->nx; g.ny = c->ny; g.nz = c->nz;
+  g.ox = c->grid.origin[0]; g.oy = c->grid.origin[1]; g.oz = c->grid.origin[2];
+  g.h = c->grid.h;
+  g.fields = c->fields;
+  g.temps = c->tA;
+  return g;
+}
+ViewArgs view_args(const wt_view* v) {
+  ViewArgs a;
+  a.uIn = v->u_in; a.vReal = v->v_real; a.cpMin = v->cp_min; a.cpMax = v->cp_max;
+  a.tMin = v->t_min; a.tMax = v->t_max; a.speedMax = v->speed_max; a.vortMax = v->vort_max;
+  return a;
+}
+}  // namespace
+
+int wt_sample_flow(wt_ctx* c, const float* pts, uint32_t n, float* out, float* vort) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (n == 0) return WT_OK;
+  if (!pts || !out) return fail(c, WT_ERR_ARG, "wt_sample_flow: null buffer");
+  float *dp = nullptr, *dout = nullptr, *dv = nullptr;
+  WT_CUDA(c, cudaMallocAsync((void**)&dp, (size_t)n * 12, c->stream));
+  WT_CUDA(c, cudaMallocAsync((void**)&dout, (size_t)n * 24, c->stream));
+  if (vort) WT_CUDA(c, cudaMallocAsync((void**)&dv, (size_t)n * 4, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(dp, pts, (size_t)n * 12, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, launch_sample_points(field_grid(c), dp, n, dout, dv, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(out, dout, (size_t)n * 24, cudaMemcpyDeviceToHost, c->stream));
+  if (vort) WT_CUDA(c, cudaMemcpyAsync(vort, dv, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaFreeAsync(dp, c->stream));
+  WT_CUDA(c, cudaFreeAsync(dout, c->stream));
+  if (dv) WT_CUDA(c, cudaFreeAsync(dv, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int wt_particles_step(wt_ctx* c, float* parts, int on_device, const wt_psim* p, const wt_view* v) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!parts || !p || !v) return fail(c, WT_ERR_ARG, "wt_particles_step: null argument");
+  if (p->count == 0) return WT_OK;
+  if (p->spawn_mode == 1u && (p->rake_rows == 0 || p->rake_cols == 0))
+    return fail(c, WT_ERR_ARG, "wt_particles_step: rake spawn needs rake_rows, rake_cols > 0");
+  PSimArgs a;
+  a.count = p->count; a.spawnMode = p->spawn_mode; a.colorMode = p->color_mode; a.frame = p->frame;
+  a.scatter = p->scatter; a.rakeRows = p->rake_rows; a.rakeCols = p->rake_cols;
+  a.dt = p->dt; a.life = p->life;
+  for (int k = 0; k < 3; k++) { a.smin[k] = p->spawn_min[k]; a.smax[k] = p->spawn_max[k]; }
+  const size_t bytes = (size_t)p->count * 32;
+  float4* d = reinterpret_cast<float4*>(parts);
+  if (!on_device) {
+    WT_CUDA(c, cudaMallocAsync((void**)&d, bytes, c->stream));
+    WT_CUDA(c, cudaMemcpyAsync(d, parts, bytes, cudaMemcpyHostToDevice, c->stream));
+  }
+  WT_CUDA(c, launch_particles(field_grid(c), a, view_args(v), d, c->stream));
+  if (!on_device) {
+    WT_CUDA(c, cudaMemcpyAsync(parts, d, bytes, cudaMemcpyDeviceToHost, c->stream));
+    WT_CUDA(c, cudaFreeAsync(d, c->stream));
+    WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return WT_OK;
+}
+
+int wt_streamlines(wt_ctx* c, const wt_stream_params* s, const wt_view* v, float* pts) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!s || !v || !pts) return fail(c, WT_ERR_ARG, "wt_streamlines: null argument");
+  if (s->lines == 0 || s->steps == 0) return WT_OK;
+  if (s->seed_mode == 1u ? (s->per_emitter == 0 || s->emitters == 0 || s->emitters > 8)
+                         : (s->rows == 0 || s->cols == 0))
+    return fail(c, WT_ERR_ARG, "wt_streamlines: seeding needs rows, cols (or 1-8 emitters and per_emitter) > 0");
+  if ((uint64_t)s->lines * s->steps >= (1ull << 31)) return fail(c, WT_ERR_ARG, "wt_streamlines: too many points");
+  StreamArgs a;
+  a.lines = s->lines; a.steps = s->steps; a.seedMode = s->seed_mode; a.colorMode = s->color_mode;
+  a.rows = s->rows; a.cols = s->cols; a.perEmitter = s->per_emitter; a.emitters = s->emitters;
+  for (int k = 0; k < 3; k++) { a.smin[k] = s->seed_min[k]; a.smax[k] = s->seed_max[k]; }
+  a.stepLen = s->step_len; a.time = s->time;
+  for (int e = 0; e < 8; e++)
+    for (int k = 0; k < 4; k++) a.emit[e][k] = s->emitter[e][k];
+  const size_t bytes = (size_t)s->lines * s->steps * 16;
+  float4* d = nullptr;
+  WT_CUDA(c, cudaMallocAsync((void**)&d, bytes, c->stream));
+  WT_CUDA(c, launch_streamlines(field_grid(c), a, view_args(v), d, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(pts, d, bytes, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaFreeAsync(d, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
   return WT_OK;
 }
 

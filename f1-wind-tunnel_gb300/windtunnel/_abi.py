@@ -71,6 +71,29 @@ class Info(ctypes.Structure):
                 ("sm_count", ctypes.c_uint32)]
 
 
+class View(ctypes.Structure):
+    """View uniform (src/engine/wgsl.ts:431-434)."""
+    _fields_ = [(n, ctypes.c_float) for n in ("u_in", "v_real", "cp_min", "cp_max", "t_min", "t_max", "speed_max",
+                                               "vort_max")]
+
+
+class PSim(ctypes.Structure):
+    """PSim uniform (wgsl.ts:517-521) as plain C fields."""
+    _fields_ = [("count", ctypes.c_uint32), ("spawn_mode", ctypes.c_uint32), ("color_mode", ctypes.c_uint32),
+                ("frame", ctypes.c_uint32), ("dt", ctypes.c_float), ("life", ctypes.c_float),
+                ("scatter", ctypes.c_uint32), ("rake_rows", ctypes.c_uint32), ("rake_cols", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("spawn_min", ctypes.c_float * 3), ("spawn_max", ctypes.c_float * 3)]
+
+
+class StreamParams(ctypes.Structure):
+    """Stream uniform and emitters (src/engine/render-wgsl.ts:521-527)."""
+    _fields_ = [("lines", ctypes.c_uint32), ("steps", ctypes.c_uint32), ("seed_mode", ctypes.c_uint32),
+                ("color_mode", ctypes.c_uint32), ("rows", ctypes.c_uint32), ("cols", ctypes.c_uint32),
+                ("per_emitter", ctypes.c_uint32), ("emitters", ctypes.c_uint32), ("seed_min", ctypes.c_float * 3),
+                ("seed_max", ctypes.c_float * 3), ("step_len", ctypes.c_float), ("time", ctypes.c_float),
+                ("emitter", (ctypes.c_float * 4) * 8)]
+
+
 _vp = ctypes.c_void_p
 _PROTOS = {
     "wt_create": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(Sim), ctypes.POINTER(_vp)]),
@@ -102,6 +125,9 @@ _PROTOS = {
     "wt_version": (ctypes.c_char_p, []),
     "wt_read_coarse": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     "wt_sdf_sample": (ctypes.c_int, [ctypes.POINTER(Shape), ctypes.POINTER(Grid), _vp]),
+    "wt_sample_flow": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp, _vp]),
+    "wt_particles_step": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(PSim), ctypes.POINTER(View)]),
+    "wt_streamlines": (ctypes.c_int, [_vp, ctypes.POINTER(StreamParams), ctypes.POINTER(View), _vp]),
 }
 
 _lib = None

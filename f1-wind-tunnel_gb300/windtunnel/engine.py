@@ -305,6 +305,32 @@ class AeroEngine:
         assert four == 4
         self._check(self.lib.wt_reset_from(self.ctx, c.ctypes.data, cx, cy, cz), "wt_reset_from")
 
+    # ---- field consumers (wgsl.ts:324-366, 516-594; render-wgsl.ts:520-576)
+    def sample_flow(self, points, vorticity=False):
+        """sampleFlow at world points [n, 3]: returns [n, 6] (ux, uy, uz, rho, temp, fluid)
+        and, if asked, vorticityAt [n]."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        n = pts.shape[0]
+        out = np.zeros((n, 6), np.float32)
+        vort = np.zeros(n, np.float32) if vorticity else None
+        self._check(self.lib.wt_sample_flow(self.ctx, pts.ctypes.data, n, out.ctypes.data,
+                                            None if vort is None else vort.ctypes.data), "wt_sample_flow")
+        return (out, vort) if vorticity else out
+
+    def particles_step(self, parts, psim, view):
+        """One particle pass over parts [count, 8] float32 (updated in place, host)."""
+        assert parts.dtype == np.float32 and parts.flags.c_contiguous and parts.shape == (psim.count, 8)
+        self._check(self.lib.wt_particles_step(self.ctx, parts.ctypes.data, 0, ctypes.byref(psim),
+                                               ctypes.byref(view)), "wt_particles_step")
+        return parts
+
+    def streamlines(self, params, view):
+        """The streamline pass: [lines, steps, 4] points (x, y, z, colour or -1)."""
+        out = np.zeros((params.lines, params.steps, 4), np.float32)
+        self._check(self.lib.wt_streamlines(self.ctx, ctypes.byref(params), ctypes.byref(view), out.ctypes.data),
+                    "wt_streamlines")
+        return out
+
     def read_coarse(self, cx, cy, cz):
         """Fluid-cell box average of the last step call's (ux, uy, uz, rho): array [cz, cy, cx, 4]."""
         out = np.empty((cz, cy, cx, 4), np.float32)

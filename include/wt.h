@@ -190,6 +190,49 @@ int wt_read_coarse(wt_ctx* ctx, uint32_t cx, uint32_t cy, uint32_t cz, float* u_
  * context (uses the current device); the warm start's geometry input. */
 int wt_sdf_sample(const wt_shape* shape, const wt_grid* grid, float* out);
 
+/* ---- field consumers: the reference's sampling, particle and streamline passes
+ * as kernels into headless buffers.  They read the (u, rho) fields of the last
+ * wt_step call and the temperatures; results are bit-identical to the
+ * reference's shaders. */
+
+/* View uniform (src/engine/wgsl.ts:431-434): colour scaling of fieldValue. */
+typedef struct wt_view {
+  float u_in, v_real, cp_min, cp_max, t_min, t_max, speed_max, vort_max;
+} wt_view;
+
+/* PSim uniform (wgsl.ts:517-521), as plain C fields. */
+typedef struct wt_psim {
+  uint32_t count, spawn_mode, color_mode, frame; /* spawn_mode 1 = rake; color_mode as fieldValue */
+  float dt, life;
+  uint32_t scatter, rake_rows, rake_cols, reserved;
+  float spawn_min[3], spawn_max[3];
+} wt_psim;
+
+/* Stream uniform and emitters (src/engine/render-wgsl.ts:521-527). */
+typedef struct wt_stream_params {
+  uint32_t lines, steps, seed_mode, color_mode; /* seed_mode 1 = ring emitters */
+  uint32_t rows, cols, per_emitter, emitters;
+  float seed_min[3], seed_max[3];
+  float step_len, time;
+  float emitter[8][4]; /* centre x, y, z and radius */
+} wt_stream_params;
+
+/* sampleFlow (wgsl.ts:332-357) at n world points (pts: n*3 floats, host):
+ * out receives n*6 floats (ux, uy, uz, rho, temperature, fluid weight); vort
+ * (may be NULL) n floats of vorticityAt (wgsl.ts:359-366). */
+int wt_sample_flow(wt_ctx* ctx, const float* pts, uint32_t n, float* out, float* vort);
+
+/* One particle pass (PARTICLES_SIM cs_main, wgsl.ts:566-594): RK2 advection,
+ * respawn and colour value of p->count particles.  parts: count*8 floats
+ * (pos x, y, z, age, step x, y, z, colour), updated in place; host memory, or
+ * device memory when parts_on_device != 0. */
+int wt_particles_step(wt_ctx* ctx, float* parts, int parts_on_device, const wt_psim* p, const wt_view* v);
+
+/* The streamline pass (STREAM_SIM cs_main, render-wgsl.ts:551-575): lines x
+ * steps points (x, y, z, colour; colour -1 once a line has ended) into pts
+ * (host, lines*steps*4 floats). */
+int wt_streamlines(wt_ctx* ctx, const wt_stream_params* s, const wt_view* v, float* pts);
+
 int wt_info_get(wt_ctx* ctx, wt_info* out);
 
 /* The context's cudaStream_t (as void*), for callers that time or order work. */

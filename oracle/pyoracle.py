@@ -69,6 +69,9 @@ def _load_ref():
     L.wtr_read.argtypes = [_vp] + [_vp] * 6 + [ctypes.c_int]
     L.wtr_write_state.argtypes = [_vp, _vp, _vp, _vp]
     L.wtr_threads.restype = ctypes.c_int
+    L.wtr_sample_flow.argtypes = [_vp, _vp, _F, _vp, _vp, _vp, ctypes.c_uint32, _vp, _vp]
+    L.wtr_particles.argtypes = [_vp, _vp, _F, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.wtr_streamlines.argtypes = [_vp, _vp, _F, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     return L
 
 
@@ -88,6 +91,56 @@ def ref_lib():
     if _R is None:
         _R = _load_ref()
     return _R
+
+
+def _grid_args(dims, origin, h):
+    return (np.ascontiguousarray(dims, np.uint32), np.ascontiguousarray(origin, np.float32), float(h))
+
+
+def ref_sample_flow(dims, origin, h, fields, temps, points):
+    """The reference's sampleFlow / vorticityAt at points [n, 3] over fields [n, 4], temps [n]."""
+    L = ref_lib()
+    d, o, hh = _grid_args(dims, origin, h)
+    f = np.ascontiguousarray(fields, np.float32)
+    t = np.ascontiguousarray(temps, np.float32)
+    p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    out = np.zeros((p.shape[0], 6), np.float32)
+    vort = np.zeros(p.shape[0], np.float32)
+    L.wtr_sample_flow(d.ctypes.data, o.ctypes.data, ctypes.c_float(hh), f.ctypes.data, t.ctypes.data, p.ctypes.data,
+                      p.shape[0], out.ctypes.data, vort.ctypes.data)
+    return out, vort
+
+
+def ref_particles(dims, origin, h, fields, temps, psim, view, parts):
+    """One reference particle pass; parts [count, 8] float32 updated in place."""
+    L = ref_lib()
+    d, o, hh = _grid_args(dims, origin, h)
+    ps = np.array([psim.count, psim.spawn_mode, psim.color_mode, psim.frame, psim.scatter, psim.rake_rows,
+                   psim.rake_cols], np.uint32)
+    pf = np.array([psim.dt, psim.life, *psim.spawn_min, *psim.spawn_max], np.float32)
+    vw = np.array([getattr(view, k) for k, _ in view._fields_], np.float32)
+    f = np.ascontiguousarray(fields, np.float32)
+    t = np.ascontiguousarray(temps, np.float32)
+    assert parts.dtype == np.float32 and parts.flags.c_contiguous
+    L.wtr_particles(d.ctypes.data, o.ctypes.data, ctypes.c_float(hh), f.ctypes.data, t.ctypes.data, ps.ctypes.data,
+                    pf.ctypes.data, vw.ctypes.data, parts.ctypes.data)
+    return parts
+
+
+def ref_streamlines(dims, origin, h, fields, temps, params, view):
+    L = ref_lib()
+    d, o, hh = _grid_args(dims, origin, h)
+    ss = np.array([params.lines, params.steps, params.seed_mode, params.color_mode, params.rows, params.cols,
+                   params.per_emitter, params.emitters], np.uint32)
+    sf = np.array([*params.seed_min, *params.seed_max, params.step_len, params.time], np.float32)
+    em = np.array([[params.emitter[e][k] for k in range(4)] for e in range(8)], np.float32)
+    vw = np.array([getattr(view, k) for k, _ in view._fields_], np.float32)
+    f = np.ascontiguousarray(fields, np.float32)
+    t = np.ascontiguousarray(temps, np.float32)
+    out = np.zeros((params.lines, params.steps, 4), np.float32)
+    L.wtr_streamlines(d.ctypes.data, o.ctypes.data, ctypes.c_float(hh), f.ctypes.data, t.ctypes.data, ss.ctypes.data,
+                      sf.ctypes.data, em.ctypes.data, vw.ctypes.data, out.ctypes.data)
+    return out
 
 
 def shape_words(shape) -> np.ndarray:

@@ -188,6 +188,81 @@ void wtr_write_state(void* p, const float* fa, const float* fields, const float*
   if (temps) memcpy(r->tA.data(), temps, n * 4);
 }
 
+// ---- field consumers: FIELD_SAMPLING, PARTICLES_SIM (wgsl.ts:324-366, 516-594) and
+// STREAM_SIM (render-wgsl.ts:520-576) over caller-provided fields / temps.
+// g: dims (3 u32), origin (3 f32), h.  view: uIn, vReal, cpMin, cpMax, tMin, tMax,
+// speedMax, vortMax.
+extern "C++" {
+template <class G>
+static void set_grid_ext(G& g, const uint32_t* dims, const float* origin, float h) {
+  g.dims = rt::vec3u(dims[0], dims[1], dims[2]);
+  g.n = dims[0] * dims[1] * dims[2];
+  g.origin = rt::vec3f(origin[0], origin[1], origin[2]);
+  g.h = h;
+}
+template <class V>
+static void set_view(V& v, const float* w) {
+  v.uIn = w[0]; v.vReal = w[1]; v.cpMin = w[2]; v.cpMax = w[3];
+  v.tMin = w[4]; v.tMax = w[5]; v.speedMax = w[6]; v.vortMax = w[7];
+}
+}  // extern "C++"
+
+// sampleFlow at n points: out[6k..6k+5] = (ux, uy, uz, rho, temp, fluid); vort[k] = vorticityAt.
+void wtr_sample_flow(const uint32_t* dims, const float* origin, float h, const float* fields, const float* temps,
+                     const float* pts, uint32_t n, float* out, float* vort) {
+  namespace M = m_particles;
+  set_grid_ext(M::grid, dims, origin, h);
+  M::fields.p = (rt::vec4f*)fields;
+  M::temps.p = (float*)temps;
+  for (uint32_t k = 0; k < n; k++) {
+    const rt::vec3f p(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]);
+    const M::Sample sm = M::sampleFlow(p);
+    out[6 * k + 0] = sm.u.x; out[6 * k + 1] = sm.u.y; out[6 * k + 2] = sm.u.z;
+    out[6 * k + 3] = sm.rho; out[6 * k + 4] = sm.temp; out[6 * k + 5] = sm.fluid;
+    if (vort) vort[k] = M::vorticityAt(p);
+  }
+}
+
+// One dispatch of the particle pass over `parts` (count x 8 floats: pos.xyzw, vel.xyzw).
+// ps: count, spawnMode, colorMode, frame, scatter, rakeRows, rakeCols (u32);
+// pf: dt, life, spawnMin[3], spawnMax[3].
+void wtr_particles(const uint32_t* dims, const float* origin, float h, const float* fields, const float* temps,
+                   const uint32_t* ps, const float* pf, const float* view, float* parts) {
+  namespace M = m_particles;
+  set_grid_ext(M::grid, dims, origin, h);
+  M::fields.p = (rt::vec4f*)fields;
+  M::temps.p = (float*)temps;
+  M::parts.p = (M::Particle*)parts;
+  M::psim.count = ps[0]; M::psim.spawnMode = ps[1]; M::psim.colorMode = ps[2]; M::psim.frame = ps[3];
+  M::psim.scatter = ps[4]; M::psim.rakeRows = ps[5]; M::psim.rakeCols = ps[6];
+  M::psim.dt = pf[0]; M::psim.life = pf[1];
+  M::psim.spawnMin = rt::vec3f(pf[2], pf[3], pf[4]);
+  M::psim.spawnMax = rt::vec3f(pf[5], pf[6], pf[7]);
+  M::psim.pad = 0.0f;
+  set_view(M::view, view);
+  dispatch(ps[0], M::cs_main_nphases, [](int ph, rt::vec3u gid, uint32_t li) { M::cs_main_run(ph, gid, li); });
+}
+
+// The streamline pass: lines x steps points (x, y, z, colour or -1) into pts.
+// ss: lines, steps, seedMode, colorMode, rows, cols, perEmitter, emitters (u32);
+// sf: seedMin[3], seedMax[3], stepLen, time; emit: 8 x (x, y, z, radius).
+void wtr_streamlines(const uint32_t* dims, const float* origin, float h, const float* fields, const float* temps,
+                     const uint32_t* ss, const float* sf, const float* emit, const float* view, float* pts) {
+  namespace M = m_stream;
+  set_grid_ext(M::grid, dims, origin, h);
+  M::fields.p = (rt::vec4f*)fields;
+  M::temps.p = (float*)temps;
+  M::pts.p = (rt::vec4f*)pts;
+  M::stream.lines = ss[0]; M::stream.steps = ss[1]; M::stream.seedMode = ss[2]; M::stream.colorMode = ss[3];
+  M::stream.rows = ss[4]; M::stream.cols = ss[5]; M::stream.perEmitter = ss[6]; M::stream.emitters = ss[7];
+  M::stream.seedMin = rt::vec3f(sf[0], sf[1], sf[2]);
+  M::stream.seedMax = rt::vec3f(sf[3], sf[4], sf[5]);
+  M::stream.stepLen = sf[6]; M::stream.time = sf[7];
+  for (int i = 0; i < 8; i++) M::emitters.e[i] = rt::vec4f(emit[4 * i], emit[4 * i + 1], emit[4 * i + 2], emit[4 * i + 3]);
+  set_view(M::view, view);
+  dispatch(ss[0], M::cs_main_nphases, [](int ph, rt::vec3u gid, uint32_t li) { M::cs_main_run(ph, gid, li); });
+}
+
 int wtr_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -318,7 +318,7 @@ def translate_module(name, wgsl, report):
             else:
                 sig = f"static {ret} {fname}({', '.join(params)})"
                 protos.append(sig + ";")
-                funcs.append(sig + " {" + stmt_rewrite(body) + "}")
+                funcs.append(sig + " {" + stmt_rewrite(ordered_constructors(body)) + "}")
             i = k
             continue
         raise SystemExit(f"{name}: cannot parse near: {code[i:i+80]!r}")
@@ -339,6 +339,26 @@ def translate_module(name, wgsl, report):
     ent.append("}")
     return "\n".join([f"namespace {name} {{", "RT_USING", *structs, *globs, *protos, *funcs, *ent,
                       f"}}  // namespace {name}", ""])
+
+
+def ordered_constructors(s):
+    """WGSL evaluates call arguments left to right; C++ leaves the order open.
+    Vector constructors whose arguments call rand() (which advances the seed it
+    points to) become braced initialisers, which C++ evaluates in order."""
+    out, i = [], 0
+    for m in re.finditer(r"\bvec[234][fiu]\(", s):
+        if m.start() < i:
+            continue
+        depth, j = 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(s[j], 0)
+            j += 1
+        args = s[m.end():j - 1]
+        if "rand(" in args:
+            out.append(s[i:m.start()] + s[m.start():m.end() - 1] + "{" + ordered_constructors(args) + "}")
+            i = j
+    out.append(s[i:])
+    return "".join(out)
 
 
 def stmt_rewrite(s):
