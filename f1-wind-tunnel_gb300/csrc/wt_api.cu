@@ -783,6 +783,66 @@ int wt_streamlines(wt_ctx* c, const wt_stream_params* s, const wt_view* v, float
   return WT_OK;
 }
 
+void wt_coef_ema_update(wt_coef_ema* e, double drag_n, double down_n, double q) {
+  if (!e || !(q > 0.0)) return;
+  const double a = e->n < 20 ? 0.15 : e->n < 60 ? 0.04 : 0.011;
+  const double r = e->n == 0 ? 1.0 : a;
+  e->cd += (drag_n / q - e->cd) * r;
+  e->cl += (down_n / q - e->cl) * r;
+  e->n++;
+}
+
+int wt_aeromap_sweep(wt_ctx* c, const wt_shape* base, const wt_sweep* s, wt_sweep_cell* out) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!base || !s || !out || !s->front || !s->rear || s->n_front == 0 || s->n_rear == 0)
+    return fail(c, WT_ERR_ARG, "wt_aeromap_sweep: empty sweep");
+  if (s->read_every == 0 || s->measure_steps < s->read_every || !(s->kmh > 0.0f))
+    return fail(c, WT_ERR_ARG, "wt_aeromap_sweep: measure_steps >= read_every > 0 and kmh > 0 required");
+  const auto even = [](uint32_t n) { return n + (n & 1u); };
+  const uint32_t every = even(s->read_every);
+  const uint32_t readings = s->measure_steps / s->read_every;
+  const double v_real = (double)s->kmh / 3.6;
+  uint32_t k = 0;
+  for (uint32_t i = 0; i < s->n_front; i++) {
+    for (uint32_t jj = 0; jj < s->n_rear; jj++, k++) {
+      const uint32_t j = (i & 1u) ? s->n_rear - 1 - jj : jj;  // aeromap.ts:79-84
+      wt_shape sh = *base;
+      sh.ride_h = s->front[i];
+      sh.rear_ride = s->rear[j];
+      if ((rc = wt_voxelize(c, &sh))) return rc;
+      wt_forces f;
+      if (s->settle_steps && (rc = wt_step(c, (int)even(s->settle_steps), 0, 0.0f))) return rc;
+      if ((rc = wt_read_forces(c, &f, 1))) return rc;  // readings of the settle phase are dropped
+      wt_sweep_cell cell = {};
+      for (uint32_t r = 0; r < readings; r++) {
+        if ((rc = wt_step(c, (int)every, 0, 0.0f)) || (rc = wt_read_forces(c, &f, 1))) return rc;
+        // engine.ts:750-753 in float, like the reference's JavaScript numbers (double)
+        const double scale = (1.0 / 10000.0 / (double)f.steps) * 1.225 * (v_real / (double)c->sim.u_in) *
+                             (v_real / (double)c->sim.u_in) * (double)c->grid.h * (double)c->grid.h * 2.0;
+        for (int g = 0; g < 3; g++) {
+          cell.group_drag_n[g] += (double)f.raw[3 * g] * scale;
+          cell.group_down_n[g] += -(double)f.raw[3 * g + 1] * scale;
+        }
+      }
+      double down = 0.0, drag = 0.0;
+      for (int g = 0; g < 3; g++) {
+        cell.group_drag_n[g] /= readings;
+        cell.group_down_n[g] /= readings;
+        down += cell.group_down_n[g];
+        drag += cell.group_drag_n[g];
+      }
+      cell.down_kg = down / 9.81;
+      cell.drag_n = drag;
+      cell.efficiency = down / (drag > 1.0 ? drag : 1.0);
+      cell.order = k;
+      cell.readings = readings;
+      out[(size_t)i * s->n_rear + j] = cell;
+    }
+  }
+  return WT_OK;
+}
+
 int wt_info_get(wt_ctx* c, wt_info* out) {
   if (!c || !out) return WT_ERR_ARG;
   out->cells = c->n;

@@ -94,6 +94,22 @@ class StreamParams(ctypes.Structure):
                 ("emitter", (ctypes.c_float * 4) * 8)]
 
 
+class CoefEma(ctypes.Structure):
+    _fields_ = [("cd", ctypes.c_double), ("cl", ctypes.c_double), ("n", ctypes.c_uint32)]
+
+
+class Sweep(ctypes.Structure):
+    _fields_ = [("n_front", ctypes.c_uint32), ("n_rear", ctypes.c_uint32), ("front", ctypes.POINTER(ctypes.c_float)),
+                ("rear", ctypes.POINTER(ctypes.c_float)), ("settle_steps", ctypes.c_uint32),
+                ("measure_steps", ctypes.c_uint32), ("read_every", ctypes.c_uint32), ("kmh", ctypes.c_float)]
+
+
+class SweepCell(ctypes.Structure):
+    _fields_ = [("down_kg", ctypes.c_double), ("drag_n", ctypes.c_double), ("efficiency", ctypes.c_double),
+                ("group_down_n", ctypes.c_double * 3), ("group_drag_n", ctypes.c_double * 3),
+                ("order", ctypes.c_uint32), ("readings", ctypes.c_uint32)]
+
+
 _vp = ctypes.c_void_p
 _PROTOS = {
     "wt_create": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(Sim), ctypes.POINTER(_vp)]),
@@ -125,6 +141,8 @@ _PROTOS = {
     "wt_version": (ctypes.c_char_p, []),
     "wt_read_coarse": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     "wt_sdf_sample": (ctypes.c_int, [ctypes.POINTER(Shape), ctypes.POINTER(Grid), _vp]),
+    "wt_coef_ema_update": (None, [ctypes.POINTER(CoefEma), ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    "wt_aeromap_sweep": (ctypes.c_int, [_vp, ctypes.POINTER(Shape), ctypes.POINTER(Sweep), _vp]),
     "wt_sample_flow": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp, _vp]),
     "wt_particles_step": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(PSim), ctypes.POINTER(View)]),
     "wt_streamlines": (ctypes.c_int, [_vp, ctypes.POINTER(StreamParams), ctypes.POINTER(View), _vp]),

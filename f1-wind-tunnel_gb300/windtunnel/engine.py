@@ -305,6 +305,19 @@ class AeroEngine:
         assert four == 4
         self._check(self.lib.wt_reset_from(self.ctx, c.ctypes.data, cx, cy, cz), "wt_reset_from")
 
+    # ---- aero-map sweep (src/ui/aeromap.ts:73-114) on this lattice
+    def aeromap_sweep(self, base_shape, front, rear, settle_steps, measure_steps, read_every=64, kmh=250.0):
+        """Serpentine ride-height sweep with re-voxelization into the running flow;
+        returns an array [n_front, n_rear] of _abi.SweepCell."""
+        fr = (ctypes.c_float * len(front))(*front)
+        re = (ctypes.c_float * len(rear))(*rear)
+        sw = _abi.Sweep(len(front), len(rear), fr, re, int(settle_steps), int(measure_steps), int(read_every),
+                        float(kmh))
+        cells = (_abi.SweepCell * (len(front) * len(rear)))()
+        self._check(self.lib.wt_aeromap_sweep(self.ctx, ctypes.byref(base_shape), ctypes.byref(sw),
+                                              ctypes.cast(cells, ctypes.c_void_p)), "wt_aeromap_sweep")
+        return [[cells[i * len(rear) + j] for j in range(len(rear))] for i in range(len(front))]
+
     # ---- field consumers (wgsl.ts:324-366, 516-594; render-wgsl.ts:520-576)
     def sample_flow(self, points, vorticity=False):
         """sampleFlow at world points [n, 3]: returns [n, 6] (ux, uy, uz, rho, temp, fluid)

@@ -190,6 +190,41 @@ int wt_read_coarse(wt_ctx* ctx, uint32_t cx, uint32_t cy, uint32_t cz, float* u_
  * context (uses the current device); the warm start's geometry input. */
 int wt_sdf_sample(const wt_shape* shape, const wt_grid* grid, float* out);
 
+/* ---- host-side averaging and the aero-map sweep (src/main.ts:586-596,
+ * src/ui/aeromap.ts:73-114), so a host UI only displays results. */
+
+/* Running body coefficients (main.ts:590-596): the first reading sets them, then
+ * an exponential average with rate 0.15 for readings 1-19, 0.04 for 20-59 and
+ * 0.011 from then on (about 12 s of readings). */
+typedef struct wt_coef_ema {
+  double cd, cl; /* drag and downforce over dynamic pressure, m^2 */
+  uint32_t n;
+} wt_coef_ema;
+void wt_coef_ema_update(wt_coef_ema* e, double drag_n, double down_n, double q);
+
+/* Aero-map sweep on one lattice, as the reference runs it: the ride-height
+ * points in serpentine order (front index i, rear index j reversed on odd i),
+ * each re-voxelized into the running flow (populations kept), settled for
+ * settle_steps, then measured over measure_steps with a force reading every
+ * read_every steps (scaled to newtons as maybeReadForces does, engine.ts:750-759,
+ * at `kmh`); cells get the mean downforce (kg), drag (N), efficiency
+ * down / max(drag, 1) and the per-group means.  Steps are rounded up to even. */
+typedef struct wt_sweep {
+  uint32_t n_front, n_rear;
+  const float* front; /* front ride heights, m (n_front) */
+  const float* rear;  /* rear ride heights, m (n_rear) */
+  uint32_t settle_steps, measure_steps, read_every;
+  float kmh;
+} wt_sweep;
+typedef struct wt_sweep_cell {
+  double down_kg, drag_n, efficiency;
+  double group_down_n[3], group_drag_n[3]; /* body, front wing, rear wing */
+  uint32_t order, readings;                /* position in the sweep; force readings averaged */
+} wt_sweep_cell;
+/* out: n_front * n_rear cells, [front][rear].  base: the shape whose ride_h and
+ * rear_ride each point replaces. */
+int wt_aeromap_sweep(wt_ctx* ctx, const wt_shape* base, const wt_sweep* s, wt_sweep_cell* out);
+
 /* ---- field consumers: the reference's sampling, particle and streamline passes
  * as kernels into headless buffers.  They read the (u, rho) fields of the last
  * wt_step call and the temperatures; results are bit-identical to the
