@@ -386,7 +386,8 @@ def main():
         return
     if fr.guarded:
         print(f"warning: {fr.guarded} cells hit the divergence guard", file=sys.stderr)
-    launches_per_frame = lbm_per_frame + (lbm_per_frame + 63) // 64 + 2
+    # per frame: the step kernels and two heat passes; one force reduction per 64 steps
+    launches_timed = args.steps * (lbm_per_frame + 2) + (args.steps * lbm_per_frame) // 64
 
     # ---- the collide-stream kernel alone: batches of kernel_steps steps, no heat
     ks = max(2, args.kernel_steps - args.kernel_steps % 2)
@@ -443,7 +444,7 @@ def main():
             },
             "cpu_baseline": base,
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches_per_frame * frames,
+            "gpu_launches": launches_timed,
             "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
         }
         print(json.dumps(line), flush=True)

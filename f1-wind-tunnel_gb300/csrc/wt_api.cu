@@ -62,10 +62,15 @@ struct wt_ctx {
   ReduceArgs* d_reduce = nullptr;          // device: this lattice's reduction record
   uint32_t bx = 128, by = 1;               // step-kernel block shape
   uint64_t version = 0;                    // bumped whenever kernel arguments change
+  // Force records of steps not yet reduced (single-lattice path): the reduction
+  // runs when pending_cap steps have accumulated or before anything reads them.
+  uint32_t pending = 0;
+  bool mass_pending = false;               // mass partials of the last field step not yet summed
   struct Graph {
     int n, heat;
     float dt;
     uint64_t version;
+    uint32_t pend0;                        // pending records when the sequence starts
     cudaGraphExec_t exec;
   };
   std::vector<Graph> graphs;               // captured wt_step sequences
@@ -186,8 +191,11 @@ ReduceArgs reduce_args(const wt_ctx* c) {
   return r;
 }
 
+int flush_forces(wt_ctx* c);
+
 // After new flags: cell words, force-carrying blocks and their partial slots.
 int rebuild_links(wt_ctx* c) {
+  if (int rc = flush_forces(c)) return rc;  // pending records use the current slot layout
   WT_CUDA(c, launch_cell_words(c->solid, c->emit, c->cellw, c->nx, c->ny, c->nz, c->stream));
   uint8_t* dflags = nullptr;
   WT_CUDA(c, cudaMallocAsync((void**)&dflags, c->geom.nblocks, c->stream));
@@ -283,16 +291,16 @@ cudaError_t enqueue_heat(wt_ctx* c, int heat_passes, float dt, cudaStream_t s) {
 // The kernels of one wt_step call: collide-stream steps (gather/local
 // alternating, fields on the last), a force reduction every pending_cap steps
 // and at the end, then the heat passes.  Pure launches: capturable in a graph.
-cudaError_t enqueue_frame(wt_ctx* c, int n, int heat_passes, float dt, cudaStream_t s) {
+cudaError_t enqueue_frame(wt_ctx* c, int n, int heat_passes, float dt, uint32_t pending0, cudaStream_t s) {
   StepArgs a = step_args(c);
-  uint32_t pending = 0;
+  uint32_t pending = pending0;
   for (int k = 0; k < n; k++) {
     const bool last = (k == n - 1);
     a.slots = c->slots + (size_t)pending * (c->nslots ? c->nslots : 1);
     cudaError_t e = launch_step(c->sim.storage, (k & 1) == 0, last, c->geom, a, s);
     if (e != cudaSuccess) return e;
     pending++;
-    if (pending == c->pending_cap || last) {
+    if (pending == c->pending_cap) {
       e = launch_force_reduce(c->d_reduce, 1, pending, last, s);
       if (e != cudaSuccess) return e;
       pending = 0;
@@ -301,10 +309,21 @@ cudaError_t enqueue_frame(wt_ctx* c, int n, int heat_passes, float dt, cudaStrea
   return enqueue_heat(c, heat_passes, dt, s);
 }
 
+// Sums the force records of the pending steps (and the mass of the last field
+// step) into the history and the totals; the deferred part of enqueue_frame.
+int flush_forces(wt_ctx* c) {
+  if (c->pending == 0 && !c->mass_pending) return WT_OK;
+  WT_CUDA(c, launch_force_reduce(c->d_reduce, 1, c->pending, c->mass_pending, c->stream));
+  c->pending = 0;
+  c->mass_pending = false;
+  return WT_OK;
+}
+
 // Launch a step sequence through a CUDA graph captured once per (n, heat, dt)
 // and argument version; WT_NO_GRAPH=1 launches the kernels directly.
 template <class Owner, class F>
-int run_graphed(Owner* o, std::vector<wt_ctx::Graph>& cache, uint64_t version, int n, int heat, float dt, F&& enqueue) {
+int run_graphed(Owner* o, std::vector<wt_ctx::Graph>& cache, uint64_t version, int n, int heat, float dt,
+                uint32_t pend0, F&& enqueue) {
   static const bool no_graph = getenv("WT_NO_GRAPH") && atoi(getenv("WT_NO_GRAPH")) != 0;
   cudaStream_t s = o->stream;
   if (no_graph) {
@@ -322,7 +341,7 @@ int run_graphed(Owner* o, std::vector<wt_ctx::Graph>& cache, uint64_t version, i
   }
   cudaGraphExec_t exec = nullptr;
   for (auto& g : cache)
-    if (g.n == n && g.heat == heat && g.dt == dt) exec = g.exec;
+    if (g.n == n && g.heat == heat && g.dt == dt && g.pend0 == pend0) exec = g.exec;
   if (!exec) {
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
@@ -337,11 +356,11 @@ int run_graphed(Owner* o, std::vector<wt_ctx::Graph>& cache, uint64_t version, i
     e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) { o->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e); return WT_ERR_CUDA; }
-    if (cache.size() >= 8) {
+    if (cache.size() >= 16) {
       cudaGraphExecDestroy(cache.front().exec);
       cache.erase(cache.begin());
     }
-    cache.push_back({n, heat, dt, version, exec});
+    cache.push_back({n, heat, dt, version, pend0, exec});
   }
   cudaError_t e = cudaGraphLaunch(exec, s);
   if (e != cudaSuccess) { o->err = std::string("cudaGraphLaunch: ") + cudaGetErrorString(e); return WT_ERR_CUDA; }
@@ -352,6 +371,9 @@ int run_graphed(Owner* o, std::vector<wt_ctx::Graph>& cache, uint64_t version, i
 int set_geometry(wt_ctx* c, uint32_t bx, uint32_t by) {
   StepGeom g = step_geometry(c->nx, c->ny, c->nz, bx, by);
   if (g.block.x == c->geom.block.x && g.block.y == c->geom.block.y) return WT_OK;
+  // Pending force records and mass partials refer to the buffers freed below:
+  // sum them first (their reduction reads block_slot's records and mass_partial).
+  if (int rc = flush_forces(c)) return rc;
   WT_CUDA(c, cudaStreamSynchronize(c->stream));
   cudaFree(c->block_slot);
   cudaFree(c->mass_partial);
@@ -482,13 +504,20 @@ int wt_set_sim(wt_ctx* c, const wt_sim* sim) {
   if (!sim) return fail(c, WT_ERR_ARG, "wt_set_sim: null sim");
   if (sim->storage != c->sim.storage) return fail(c, WT_ERR_ARG, "wt_set_sim: storage format is fixed at wt_create");
   if (!valid_tau(*sim, c->nx)) return fail(c, WT_ERR_ARG, "wt_set_sim: relaxation time below 2^-10 or not finite");
+  // Identical parameters (syncSim runs every frame) still upload the per-x table,
+  // but leave the kernel arguments - and so the captured step sequences - valid.
+  const bool same = memcmp(&c->sim, sim, sizeof(wt_sim)) == 0;
+  const uint64_t version = c->version;
   c->sim = *sim;
-  return apply_sim(c);
+  if ((rc = apply_sim(c))) return rc;
+  if (same) c->version = version;
+  return WT_OK;
 }
 
 int wt_reset(wt_ctx* c) {
   int rc = check_ctx(c);
   if (rc) return rc;
+  if ((rc = flush_forces(c))) return rc;
   WT_CUDA(c, launch_init(c->sim.storage, c->pop, c->fields, c->outlet_u, c->nx, c->ny, c->nz, c->np, c->sim.u_in, c->stream));
   WT_CUDA(c, cudaMemsetAsync(c->tA, 0, c->n * 4, c->stream));
   WT_CUDA(c, cudaMemsetAsync(c->tB, 0, c->n * 4, c->stream));
@@ -529,9 +558,14 @@ int wt_step(wt_ctx* c, int n_lbm_steps, int heat_passes, float heat_dt) {
     return fail(c, WT_ERR_ARG, "wt_step: n_lbm_steps must be even and >= 2 (the engine issues max(2, steps - steps % 2))");
   if (heat_passes < 0 || (heat_passes & 1)) return fail(c, WT_ERR_ARG, "wt_step: heat_passes must be 0 or even");
   const float dt = heat_dt > 0.0f ? heat_dt : (float)n_lbm_steps / 2.0f;
-  if ((rc = run_graphed(c, c->graphs, c->version, n_lbm_steps, heat_passes, dt,
-                        [&](cudaStream_t s) { return enqueue_frame(c, n_lbm_steps, heat_passes, dt, s); })))
+  const uint32_t pend0 = c->pending;
+  if ((rc = run_graphed(c, c->graphs, c->version, n_lbm_steps, heat_passes, dt, pend0,
+                        [&](cudaStream_t s) { return enqueue_frame(c, n_lbm_steps, heat_passes, dt, pend0, s); })))
     return rc;
+  // the host copy of enqueue_frame's pending count
+  const uint32_t total = pend0 + (uint32_t)n_lbm_steps;
+  c->pending = total % c->pending_cap;
+  c->mass_pending = (c->pending != 0);  // a reduction on the last step summed the mass too
   c->steps_total += n_lbm_steps;
   c->steps_since_read += n_lbm_steps;
   c->steps_recorded += n_lbm_steps;
@@ -542,6 +576,7 @@ int wt_read_forces(wt_ctx* c, wt_forces* out, int reset) {
   int rc = check_ctx(c);
   if (rc) return rc;
   if (!out) return fail(c, WT_ERR_ARG, "wt_read_forces: null output");
+  if ((rc = flush_forces(c))) return rc;
   double tot[18];
   unsigned int g = 0;
   WT_CUDA(c, cudaMemcpyAsync(tot, c->totals, sizeof(tot), cudaMemcpyDeviceToHost, c->stream));
@@ -564,6 +599,7 @@ int wt_read_forces(wt_ctx* c, wt_forces* out, int reset) {
 int wt_read_force_history(wt_ctx* c, double* out, uint32_t count) {
   int rc = check_ctx(c);
   if (rc) return rc;
+  if ((rc = flush_forces(c))) return rc;
   if (!out && count) return fail(c, WT_ERR_ARG, "wt_read_force_history: null output");
   const uint64_t avail = c->steps_recorded < WT_HIST_CAP ? c->steps_recorded : WT_HIST_CAP;
   if (count > avail) return fail(c, WT_ERR_ARG, "wt_read_force_history: only " + std::to_string(avail) + " steps recorded");
@@ -621,6 +657,7 @@ int wt_read_populations(wt_ctx* c, float* f) {
 int wt_write_state(wt_ctx* c, const float* f, const float* u_rho, const float* temps) {
   int rc = check_ctx(c);
   if (rc) return rc;
+  if ((rc = flush_forces(c))) return rc;
   if (f) {
     float* tmp = nullptr;
     WT_CUDA(c, cudaMallocAsync((void**)&tmp, c->n * 19 * 4, c->stream));
@@ -647,6 +684,7 @@ int wt_write_state(wt_ctx* c, const float* f, const float* u_rho, const float* t
 int wt_reset_from(wt_ctx* c, const float* u_rho, uint32_t cx, uint32_t cy, uint32_t cz) {
   int rc = check_ctx(c);
   if (rc) return rc;
+  if ((rc = flush_forces(c))) return rc;
   if (!u_rho || cx == 0 || cy == 0 || cz == 0) return fail(c, WT_ERR_ARG, "wt_reset_from: empty coarse field");
   float4* tmp = nullptr;
   const size_t bytes = (size_t)cx * cy * cz * 16;
@@ -889,6 +927,7 @@ struct Saved {
 };
 
 int save_state(wt_ctx* c, Saved& sv) {
+  if (int rc = flush_forces(c)) return rc;
   const size_t pb = 19 * c->np * c->elem;
   WT_CUDA(c, cudaMallocAsync(&sv.pop, pb, c->stream));
   WT_CUDA(c, cudaMallocAsync((void**)&sv.fields, c->n * 16, c->stream));
@@ -917,6 +956,8 @@ int restore_state(wt_ctx* c, Saved& sv) {
   WT_CUDA(c, cudaFreeAsync(sv.fields, c->stream));
   WT_CUDA(c, cudaFreeAsync(sv.outlet, c->stream));
   WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->pending = 0;  // the trial steps' records are dropped with them
+  c->mass_pending = false;
   return WT_OK;
 }
 
@@ -1118,7 +1159,9 @@ int wt_batch_step(wt_batch* b, int n_lbm_steps, int heat_passes, float heat_dt) 
   int rc = refresh_batch(b);
   if (rc) return rc;
   const float dt = heat_dt > 0.0f ? heat_dt : (float)n_lbm_steps / 2.0f;
-  if ((rc = run_graphed(b, b->graphs, b->version, n_lbm_steps, heat_passes, dt,
+  for (auto* c : b->lat)
+    if ((rc = flush_forces(c))) return bfail(b, rc, c->err);
+  if ((rc = run_graphed(b, b->graphs, b->version, n_lbm_steps, heat_passes, dt, 0u,
                         [&](cudaStream_t s) { return enqueue_batch(b, n_lbm_steps, heat_passes, dt, s); })))
     return rc;
   for (auto* c : b->lat) {

@@ -887,7 +887,7 @@ cudaError_t launch_batch_step(uint32_t storage, bool gather, bool write_fields, 
 
 cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t nsteps, bool with_mass,
                                 cudaStream_t s) {
-  if (nsteps == 0 || count == 0) return cudaSuccess;
+  if ((nsteps == 0 && !with_mass) || count == 0) return cudaSuccess;
   force_reduce_kernel<<<dim3(nsteps + 1, count), RED_THREADS, 0, s>>>(args, nsteps, with_mass ? 1u : 0u);
   return cudaGetLastError();
 }
