@@ -13,6 +13,7 @@
 #include "wt_fmath.h"
 #include "wt_internal.h"
 #include "wt_fields.h"
+#include "wt_render.h"
 #include "wt_lattice.cuh"
 
 using namespace wt;
@@ -74,6 +75,7 @@ struct wt_ctx {
     cudaGraphExec_t exec;
   };
   std::vector<Graph> graphs;               // captured wt_step sequences
+  wt_shape shape{WT_KIND_EMPTY};           // last voxelized shape (the renderer's scene)
   std::string err;
 };
 
@@ -535,6 +537,7 @@ int wt_voxelize(wt_ctx* c, const wt_shape* shape) {
     return fail(c, WT_ERR_UNSUPPORTED, "wt_voxelize: scene kind " + std::to_string(k) +
                                            " is not built (custom profile and baked-mesh scenes)");
   WT_CUDA(c, launch_voxelize(*shape, c->grid, c->solid, c->emit, c->stream));
+  c->shape = *shape;
   return rebuild_links(c);
 }
 
@@ -1214,3 +1217,266 @@ void* wt_batch_stream(wt_batch* b) { return b ? (void*)b->stream : nullptr; }
 const char* wt_batch_last_error(const wt_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- renderer
+struct wt_renderer {
+  wt_ctx* c = nullptr;
+  uint32_t w = 0, h = 0, hw = 0, hh = 0;
+  ushort4* scene = nullptr;
+  ushort4* hist[2] = {nullptr, nullptr};
+  ushort4* glow = nullptr;
+  ushort4* bloom_a = nullptr;
+  ushort4* bloom_b = nullptr;
+  uchar4* out = nullptr;
+  unsigned long long* acc = nullptr;  // glow fixed-point sums, w*h*4
+  float4* staging = nullptr;          // host particle / line data copied for a draw
+  size_t staging_bytes = 0;
+};
+
+namespace {
+F3 f3(const float* v) { return F3{v[0], v[1], v[2]}; }
+F3 f3n(float x, float y, float z) {  // normalize(e) = e / length(e), IEEE operations
+  const float l = sqrtf(x * x + y * y + z * z);
+  return F3{x / l, y / l, z / l};
+}
+int render_check(wt_renderer* r) {
+  if (!r || !r->c) return WT_ERR_ARG;
+  return check_ctx(r->c);
+}
+void* target_ptr(wt_renderer* r, int t, size_t* bytes) {
+  const size_t full = (size_t)r->w * r->h, half = (size_t)r->hw * r->hh;
+  switch (t) {
+    case WT_TARGET_SCENE: *bytes = full * 8; return r->scene;
+    case WT_TARGET_HIST0: *bytes = full * 8; return r->hist[0];
+    case WT_TARGET_HIST1: *bytes = full * 8; return r->hist[1];
+    case WT_TARGET_GLOW: *bytes = full * 8; return r->glow;
+    case WT_TARGET_BLOOM_A: *bytes = half * 8; return r->bloom_a;
+    case WT_TARGET_BLOOM_B: *bytes = half * 8; return r->bloom_b;
+    case WT_TARGET_OUTPUT: *bytes = full * 4; return r->out;
+    default: *bytes = 0; return nullptr;
+  }
+}
+// Device copy of caller data for a draw: the pointer itself, or host data staged
+// into the renderer's buffer (region `slot` of two, each `bytes` long).
+int draw_source(wt_renderer* r, const float* p, int on_device, size_t bytes, size_t offset, const float4** out) {
+  wt_ctx* c = r->c;
+  if (on_device) {
+    *out = reinterpret_cast<const float4*>(p);
+    return WT_OK;
+  }
+  WT_CUDA(c, cudaMemcpyAsync(reinterpret_cast<char*>(r->staging) + offset, p, bytes, cudaMemcpyHostToDevice, c->stream));
+  *out = reinterpret_cast<const float4*>(reinterpret_cast<char*>(r->staging) + offset);
+  return WT_OK;
+}
+}  // namespace
+
+void wt_render_destroy(wt_renderer* r) {
+  if (!r) return;
+  if (r->c) cudaStreamSynchronize(r->c->stream);
+  void* bufs[] = {r->scene, r->hist[0], r->hist[1], r->glow, r->bloom_a, r->bloom_b, r->out, r->acc, r->staging};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  delete r;
+}
+
+int wt_render_create(wt_ctx* c, uint32_t width, uint32_t height, wt_renderer** out) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!out) return fail(c, WT_ERR_ARG, "wt_render_create: null output");
+  *out = nullptr;
+  if (width == 0 || height == 0 || width > 16384 || height > 16384)
+    return fail(c, WT_ERR_ARG, "wt_render_create: width and height must be 1..16384");
+  wt_renderer* r = new wt_renderer;
+  r->c = c;
+  r->w = width;
+  r->h = height;
+  r->hw = width >> 1 ? width >> 1 : 1;   // engine.ts:291: max(1, w >> 1)
+  r->hh = height >> 1 ? height >> 1 : 1;
+  const size_t full = (size_t)width * height, half = (size_t)r->hw * r->hh;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+  };
+  alloc((void**)&r->scene, full * 8);
+  alloc((void**)&r->hist[0], full * 8);
+  alloc((void**)&r->hist[1], full * 8);
+  alloc((void**)&r->glow, full * 8);
+  alloc((void**)&r->bloom_a, half * 8);
+  alloc((void**)&r->bloom_b, half * 8);
+  alloc((void**)&r->out, full * 4);
+  alloc((void**)&r->acc, full * 32);
+  if (e != cudaSuccess) {
+    wt_render_destroy(r);
+    return fail(c, e == cudaErrorMemoryAllocation ? WT_ERR_NOMEM : WT_ERR_CUDA,
+                std::string("wt_render_create: ") + cudaGetErrorString(e));
+  }
+  *out = r;
+  return WT_OK;
+}
+
+int wt_render_scene(wt_renderer* r, const wt_cam* cam, const wt_look* look, const wt_view* view) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  if (!cam || !look || !view) return fail(c, WT_ERR_ARG, "wt_render_scene: null argument");
+  if (look->mesh_mode != 0u)
+    return fail(c, WT_ERR_UNSUPPORTED, "wt_render_scene: the baked-mesh G-buffer path (mesh_mode) is not built");
+  SceneArgs a;
+  a.shape = c->shape;
+  a.g = field_grid(c);
+  a.view = view_args(view);
+  a.pos = f3(cam->pos); a.fwd = f3(cam->fwd); a.right = f3(cam->right); a.up = f3(cam->up);
+  a.tan_half = cam->tan_half; a.aspect = cam->aspect; a.time = cam->time; a.road_speed = cam->road_speed;
+  a.jitter_x = cam->jitter[0]; a.jitter_y = cam->jitter[1];
+  a.bmin = f3(look->bmin); a.bmax = f3(look->bmax);
+  // toLinear (render-wgsl.ts:40) of the livery colours, once per frame: the same
+  // function the shader evaluates per hit, so the same bits
+  a.paint_lin = F3{wtm::powf(look->paint[0], 2.2f), wtm::powf(look->paint[1], 2.2f), wtm::powf(look->paint[2], 2.2f)};
+  a.accent_lin = F3{wtm::powf(look->accent[0], 2.2f), wtm::powf(look->accent[1], 2.2f), wtm::powf(look->accent[2], 2.2f)};
+  a.surf_mode = look->surf_mode; a.palette = look->palette; a.carbon_body = look->carbon_body; a.is_f1 = look->is_f1;
+  a.slice_axis = look->slice_axis; a.show_flow = look->show_flow;
+  a.slice_pos = look->slice_pos; a.slice_alpha = look->slice_alpha;
+  a.key = f3n(-0.32f, 0.90f, 0.30f);    // KEY (render-wgsl.ts:38)
+  a.fill_a = f3n(0.6f, 0.35f, -0.7f);   // shadeSurface fill lights (render-wgsl.ts:265)
+  a.fill_b = f3n(0.6f, 0.35f, 0.7f);
+  a.w = r->w; a.h = r->h;
+  a.scene = r->scene;
+  WT_CUDA(c, launch_render_scene(a, c->stream));
+  return WT_OK;
+}
+
+int wt_render_taa(wt_renderer* r, const wt_taa* t, int cur) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  if (!t || (cur != 0 && cur != 1)) return fail(c, WT_ERR_ARG, "wt_render_taa: null uniform or cur not 0/1");
+  TaaArgs a;
+  for (int i = 0; i < 16; i++) a.m[i] = t->prev_view_proj[i];
+  a.cam_pos = f3(t->cam_pos); a.fwd = f3(t->fwd); a.right = f3(t->right); a.up = f3(t->up);
+  a.tan_half = t->tan_half; a.aspect = t->aspect; a.blend = t->blend;
+  a.w = r->w; a.h = r->h;
+  a.cur = r->scene;
+  a.hist = r->hist[1 - cur];
+  a.out = r->hist[cur];
+  WT_CUDA(c, launch_taa(a, c->stream));
+  return WT_OK;
+}
+
+int wt_render_glow(wt_renderer* r, const float* parts, int parts_on_device, const wt_pdraw* pd, const float* pts,
+                   int pts_on_device, const wt_sdraw* sd) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  if ((parts && !pd) || (pts && !sd)) return fail(c, WT_ERR_ARG, "wt_render_glow: draw data without its uniform");
+  if (pts && sd->steps < 2) return fail(c, WT_ERR_ARG, "wt_render_glow: streamlines need steps >= 2");
+  const size_t texels = (size_t)r->w * r->h;
+  const size_t pbytes = parts ? (size_t)pd->count * 32 : 0, sbytes = pts ? (size_t)sd->lines * sd->steps * 16 : 0;
+  const uint64_t pinst = parts ? 2ull * pd->count : 0, sinst = pts ? (uint64_t)sd->lines * 2ull * (sd->steps - 1u) : 0;
+  if (pinst >= (1ull << 31) || sinst >= (1ull << 31)) return fail(c, WT_ERR_ARG, "wt_render_glow: too many instances");
+  const size_t need = (parts_on_device ? 0 : pbytes) + (pts_on_device ? 0 : sbytes);
+  if (need > r->staging_bytes) {
+    WT_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (r->staging) cudaFree(r->staging);
+    r->staging = nullptr;
+    r->staging_bytes = 0;
+    WT_CUDA(c, cudaMalloc((void**)&r->staging, need));
+    r->staging_bytes = need;
+  }
+  WT_CUDA(c, cudaMemsetAsync(r->acc, 0, texels * 32, c->stream));
+  auto base = [&](DrawArgs& d) {
+    d.w = r->w; d.h = r->h;
+    d.scene = r->scene;
+    d.acc = r->acc;
+  };
+  size_t off = 0;
+  if (parts && pinst) {
+    DrawArgs d{};
+    base(d);
+    d.kind = 0;
+    for (int i = 0; i < 16; i++) d.m[i] = pd->view_proj[i];
+    d.cam_pos = f3(pd->cam_pos);
+    d.width = pd->width; d.res_x = pd->res[0]; d.res_y = pd->res[1];
+    d.trail = pd->trail; d.alpha = pd->alpha; d.fade_in = pd->fade_in;
+    d.count = pd->count; d.palette = pd->palette;
+    d.instances = (uint32_t)pinst;
+    if ((rc = draw_source(r, parts, parts_on_device, pbytes, off, &d.data))) return rc;
+    if (!parts_on_device) off += pbytes;
+    WT_CUDA(c, launch_glow_draw(d, c->stream));
+  }
+  if (pts && sinst) {
+    DrawArgs d{};
+    base(d);
+    d.kind = 1;
+    for (int i = 0; i < 16; i++) d.m[i] = sd->view_proj[i];
+    d.cam_pos = f3(sd->cam_pos);
+    d.width = sd->width; d.res_x = sd->res[0]; d.res_y = sd->res[1];
+    d.time = sd->time; d.intensity = sd->intensity; d.pulse = sd->pulse;
+    d.lines = sd->lines; d.steps = sd->steps; d.palette = sd->palette;
+    d.instances = (uint32_t)sinst;
+    if ((rc = draw_source(r, pts, pts_on_device, sbytes, off, &d.data))) return rc;
+    WT_CUDA(c, launch_glow_draw(d, c->stream));
+  }
+  WT_CUDA(c, launch_glow_resolve(r->acc, r->glow, (uint32_t)texels, c->stream));
+  return WT_OK;
+}
+
+int wt_render_bloom(wt_renderer* r) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  BlurArgs a;
+  for (int k = -6; k <= 6; k++) a.wk[k + 6] = wtm::expf(-(float)(k * k) / 14.0f);
+  a.gain = 1.0f;
+  // engine.ts:316: glow (full size) -> bloom A (half size), dir (1, 0), spacing 3
+  a.dir_x = 1.0f; a.dir_y = 0.0f; a.spacing = 3.0f;
+  a.sw = r->w; a.sh = r->h; a.dw = r->hw; a.dh = r->hh;
+  a.src = r->glow; a.dst = r->bloom_a;
+  WT_CUDA(c, launch_blur(a, c->stream));
+  // engine.ts:317: bloom A -> bloom B, dir (0, 1), spacing 1.5
+  a.dir_x = 0.0f; a.dir_y = 1.0f; a.spacing = 1.5f;
+  a.sw = r->hw; a.sh = r->hh;
+  a.src = r->bloom_a; a.dst = r->bloom_b;
+  WT_CUDA(c, launch_blur(a, c->stream));
+  return WT_OK;
+}
+
+int wt_render_present(wt_renderer* r, const wt_post* post, int cur) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  if (!post || (cur != 0 && cur != 1)) return fail(c, WT_ERR_ARG, "wt_render_present: null uniform or cur not 0/1");
+  PresentArgs a;
+  a.bloom = post->bloom; a.exposure = post->exposure;
+  a.w = r->w; a.h = r->h; a.gw = r->w; a.gh = r->h; a.bw = r->hw; a.bh = r->hh;
+  a.scene = r->hist[cur];
+  a.glow = r->glow;
+  a.bloom_tex = r->bloom_b;
+  a.out = r->out;
+  WT_CUDA(c, launch_present(a, c->stream));
+  return WT_OK;
+}
+
+int wt_render_read(wt_renderer* r, int target, void* host) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  size_t bytes = 0;
+  void* p = target_ptr(r, target, &bytes);
+  if (!p || !host) return fail(c, WT_ERR_ARG, "wt_render_read: unknown target or null buffer");
+  WT_CUDA(c, cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+int wt_render_write(wt_renderer* r, int target, const void* host) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  size_t bytes = 0;
+  void* p = target_ptr(r, target, &bytes);
+  if (!p || !host) return fail(c, WT_ERR_ARG, "wt_render_write: unknown target or null buffer");
+  WT_CUDA(c, cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}

@@ -110,6 +110,49 @@ class SweepCell(ctypes.Structure):
                 ("order", ctypes.c_uint32), ("readings", ctypes.c_uint32)]
 
 
+_F = ctypes.c_float
+_U = ctypes.c_uint32
+
+
+class Cam(ctypes.Structure):
+    """Cam uniform (src/engine/render-wgsl.ts:5-11)."""
+    _fields_ = [("pos", _F * 3), ("tan_half", _F), ("fwd", _F * 3), ("aspect", _F), ("right", _F * 3), ("time", _F),
+                ("up", _F * 3), ("road_speed", _F), ("jitter", _F * 2), ("pad0", _F), ("pad1", _F)]
+
+
+class Look(ctypes.Structure):
+    """Look uniform (render-wgsl.ts:12-19)."""
+    _fields_ = [("bmin", _F * 3), ("surf_mode", _U), ("bmax", _F * 3), ("palette", _U), ("paint", _F * 3),
+                ("carbon_body", _U), ("accent", _F * 3), ("is_f1", _U), ("slice_axis", _U), ("slice_pos", _F),
+                ("slice_alpha", _F), ("show_flow", _U), ("mesh_mode", _U), ("cooling", _U), ("pad1", _U),
+                ("pad2", _U)]
+
+
+class Taa(ctypes.Structure):
+    """Taa uniform (render-wgsl.ts:457-463)."""
+    _fields_ = [("prev_view_proj", _F * 16), ("cam_pos", _F * 3), ("tan_half", _F), ("fwd", _F * 3),
+                ("aspect", _F), ("right", _F * 3), ("blend", _F), ("up", _F * 3), ("pad", _F)]
+
+
+class PDraw(ctypes.Structure):
+    """PDraw uniform (src/engine/wgsl.ts:598-603)."""
+    _fields_ = [("view_proj", _F * 16), ("cam_pos", _F * 3), ("width", _F), ("res", _F * 2), ("trail", _F),
+                ("alpha", _F), ("count", _U), ("palette", _U), ("fade_in", _F), ("pad", _F)]
+
+
+class SDraw(ctypes.Structure):
+    """SDraw uniform (render-wgsl.ts:579-584)."""
+    _fields_ = [("view_proj", _F * 16), ("cam_pos", _F * 3), ("width", _F), ("res", _F * 2), ("time", _F),
+                ("intensity", _F), ("lines", _U), ("steps", _U), ("palette", _U), ("pulse", _F)]
+
+
+class Post(ctypes.Structure):
+    """Post uniform (render-wgsl.ts:421)."""
+    _fields_ = [("bloom", _F), ("exposure", _F), ("pad0", _F), ("pad1", _F)]
+
+
+TARGET_SCENE, TARGET_HIST0, TARGET_HIST1, TARGET_GLOW, TARGET_BLOOM_A, TARGET_BLOOM_B, TARGET_OUTPUT = range(7)
+
 _vp = ctypes.c_void_p
 _PROTOS = {
     "wt_create": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(Sim), ctypes.POINTER(_vp)]),
@@ -146,6 +189,16 @@ _PROTOS = {
     "wt_sample_flow": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp, _vp]),
     "wt_particles_step": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(PSim), ctypes.POINTER(View)]),
     "wt_streamlines": (ctypes.c_int, [_vp, ctypes.POINTER(StreamParams), ctypes.POINTER(View), _vp]),
+    "wt_render_create": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_vp)]),
+    "wt_render_destroy": (None, [_vp]),
+    "wt_render_scene": (ctypes.c_int, [_vp, ctypes.POINTER(Cam), ctypes.POINTER(Look), ctypes.POINTER(View)]),
+    "wt_render_taa": (ctypes.c_int, [_vp, ctypes.POINTER(Taa), ctypes.c_int]),
+    "wt_render_glow": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(PDraw), _vp, ctypes.c_int,
+                                      ctypes.POINTER(SDraw)]),
+    "wt_render_bloom": (ctypes.c_int, [_vp]),
+    "wt_render_present": (ctypes.c_int, [_vp, ctypes.POINTER(Post), ctypes.c_int]),
+    "wt_render_read": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "wt_render_write": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
 }
 
 _lib = None

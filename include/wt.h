@@ -268,6 +268,100 @@ int wt_particles_step(wt_ctx* ctx, float* parts, int parts_on_device, const wt_p
  * (host, lines*steps*4 floats). */
 int wt_streamlines(wt_ctx* ctx, const wt_stream_params* s, const wt_view* v, float* pts);
 
+/* ---- render passes: the reference's frame graph into headless render targets
+ * (src/engine/render-wgsl.ts; targets engine.ts:290-306, passes engine.ts:714-725).
+ * The uniform structs below have the layouts of the WGSL uniforms they replace.
+ * A renderer reads the fields and temperatures of its context's last step call
+ * and the shape of its last wt_voxelize; its passes are queued on the
+ * context's stream and return at once.  The baked-mesh G-buffer path
+ * (look.mesh_mode != 0) is not built. */
+
+/* Cam uniform (render-wgsl.ts:5-11). */
+typedef struct wt_cam {
+  float pos[3], tan_half;
+  float fwd[3], aspect;
+  float right[3], time;
+  float up[3], road_speed;
+  float jitter[2], pad0, pad1;
+} wt_cam;
+
+/* Look uniform (render-wgsl.ts:12-19); palette as fieldValue's colour field. */
+typedef struct wt_look {
+  float bmin[3]; uint32_t surf_mode;
+  float bmax[3]; uint32_t palette;
+  float paint[3]; uint32_t carbon_body;
+  float accent[3]; uint32_t is_f1;
+  uint32_t slice_axis; float slice_pos, slice_alpha; uint32_t show_flow;
+  uint32_t mesh_mode, cooling, pad1, pad2;
+} wt_look;
+
+/* Taa uniform (render-wgsl.ts:457-463); matrices column-major. */
+typedef struct wt_taa {
+  float prev_view_proj[16];
+  float cam_pos[3], tan_half;
+  float fwd[3], aspect;
+  float right[3], blend;
+  float up[3], pad;
+} wt_taa;
+
+/* PDraw uniform (src/engine/wgsl.ts:598-603). */
+typedef struct wt_pdraw {
+  float view_proj[16];
+  float cam_pos[3], width;
+  float res[2], trail, alpha;
+  uint32_t count, palette; float fade_in, pad;
+} wt_pdraw;
+
+/* SDraw uniform (render-wgsl.ts:579-584). */
+typedef struct wt_sdraw {
+  float view_proj[16];
+  float cam_pos[3], width;
+  float res[2], time, intensity;
+  uint32_t lines, steps, palette; float pulse;
+} wt_sdraw;
+
+/* Post uniform (render-wgsl.ts:421). */
+typedef struct wt_post {
+  float bloom, exposure, pad0, pad1;
+} wt_post;
+
+/* Render targets, for wt_render_read / wt_render_write.  Float targets hold
+ * RGBA binary16 (4 uint16 per texel); WT_TARGET_OUTPUT holds RGBA8. */
+enum {
+  WT_TARGET_SCENE = 0,   /* width x height, RENDER output (alpha: hit distance) */
+  WT_TARGET_HIST0 = 1,   /* width x height, TAA history 0 */
+  WT_TARGET_HIST1 = 2,   /* width x height, TAA history 1 */
+  WT_TARGET_GLOW = 3,    /* width x height, particles and streamlines */
+  WT_TARGET_BLOOM_A = 4, /* half size, horizontal blur */
+  WT_TARGET_BLOOM_B = 5, /* half size, vertical blur */
+  WT_TARGET_OUTPUT = 6   /* width x height, presented RGBA8 */
+};
+
+typedef struct wt_renderer wt_renderer;
+
+/* Targets of one view: width x height (half-size bloom targets, at least 1x1). */
+int wt_render_create(wt_ctx* ctx, uint32_t width, uint32_t height, wt_renderer** out);
+void wt_render_destroy(wt_renderer* r);
+/* RENDER pass (render-wgsl.ts:288-398) into WT_TARGET_SCENE. */
+int wt_render_scene(wt_renderer* r, const wt_cam* cam, const wt_look* look, const wt_view* view);
+/* TAA resolve (render-wgsl.ts:456-518): scene and history 1-cur into history cur. */
+int wt_render_taa(wt_renderer* r, const wt_taa* taa, int cur);
+/* Glow pass (engine.ts:719-722): clear, then the particle quads (parts: pd->count
+ * particles of 8 floats, drawn twice, mirrored; NULL = no draw) and the
+ * streamline quads (pts: sd->lines * sd->steps points of 4 floats, drawn
+ * lines * 2 * (steps - 1) times; NULL = no draw).  Host memory, or device
+ * memory when the matching *_on_device flag is set. */
+int wt_render_glow(wt_renderer* r, const float* parts, int parts_on_device, const wt_pdraw* pd, const float* pts,
+                   int pts_on_device, const wt_sdraw* sd);
+/* Bloom (engine.ts:316-317): BLUR (1, 0) spacing 3 glow -> bloom A, then
+ * (0, 1) spacing 1.5 bloom A -> bloom B, gain 1. */
+int wt_render_bloom(wt_renderer* r);
+/* PRESENT (render-wgsl.ts:442-454): history cur, glow and bloom B -> output. */
+int wt_render_present(wt_renderer* r, const wt_post* post, int cur);
+/* Copy a target to / from host memory (synchronous). */
+int wt_render_read(wt_renderer* r, int target, void* host);
+int wt_render_write(wt_renderer* r, int target, const void* host);
+
 int wt_info_get(wt_ctx* ctx, wt_info* out);
 
 /* The context's cudaStream_t (as void*), for callers that time or order work. */

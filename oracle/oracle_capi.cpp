@@ -111,9 +111,18 @@ uint64_t wto_guarded(void* h) {
   with(h, [&](auto& L) { g = L.guarded; });
   return g;
 }
-// The project's sin/cos/atan (wt_fmath.h) on an array, for accuracy tests: which 0 sin, 1 cos, 2 atan.
+// The project's math functions (wt_fmath.h) on an array, for accuracy tests:
+// which 0 sin, 1 cos, 2 atan, 3 exp, 4 exp2, 5 log2.
 void wto_fmath(int which, const float* x, float* y, int n) {
-  for (int i = 0; i < n; i++) y[i] = which == 0 ? wtm::sinf(x[i]) : which == 1 ? wtm::cosf(x[i]) : wtm::atanf(x[i]);
+  for (int i = 0; i < n; i++) {
+    const float v = x[i];
+    y[i] = which == 0 ? wtm::sinf(v) : which == 1 ? wtm::cosf(v) : which == 2 ? wtm::atanf(v)
+         : which == 3 ? wtm::expf(v) : which == 4 ? wtm::exp2f(v) : wtm::log2f(v);
+  }
+}
+// Two-argument functions: which 0 pow(x, y), 1 atan2(x, y) (x = the ordinate).
+void wto_fmath2(int which, const float* x, const float* y, float* out, int n) {
+  for (int i = 0; i < n; i++) out[i] = which == 0 ? wtm::powf(x[i], y[i]) : wtm::atan2f(x[i], y[i]);
 }
 int wto_threads(void) {
 #ifdef _OPENMP

@@ -72,6 +72,12 @@ def _load_ref():
     L.wtr_sample_flow.argtypes = [_vp, _vp, _F, _vp, _vp, _vp, ctypes.c_uint32, _vp, _vp]
     L.wtr_particles.argtypes = [_vp, _vp, _F, _vp, _vp, _vp, _vp, _vp, _vp]
     L.wtr_streamlines.argtypes = [_vp, _vp, _F, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+    _i = ctypes.c_int
+    L.wtr_render_scene.argtypes = [_vp, _vp, _F, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp]
+    L.wtr_taa.argtypes = [_vp, _vp, _i, _i, _vp, _vp]
+    L.wtr_blur.argtypes = [_vp, _i, _i, _vp, _i, _i, _vp]
+    L.wtr_present.argtypes = [_vp, _i, _i, _vp, _i, _i, _vp, _i, _i, _vp, _vp]
+    L.wtr_glow.argtypes = [_vp, _i, _i, _vp, _vp, ctypes.c_uint32, _vp, _vp, ctypes.c_uint32, _vp]
     return L
 
 
@@ -140,6 +146,71 @@ def ref_streamlines(dims, origin, h, fields, temps, params, view):
     out = np.zeros((params.lines, params.steps, 4), np.float32)
     L.wtr_streamlines(d.ctypes.data, o.ctypes.data, ctypes.c_float(hh), f.ctypes.data, t.ctypes.data, ss.ctypes.data,
                       sf.ctypes.data, em.ctypes.data, vw.ctypes.data, out.ctypes.data)
+    return out
+
+
+# ---- render passes (src/engine/render-wgsl.ts) through the translated shaders.
+# Uniform arguments are the ctypes structs of windtunnel._abi (Cam, Look, Taa,
+# PDraw, SDraw, Post), whose layouts are the WGSL uniforms'.  Targets are float32
+# arrays [h, w, 4] holding binary16-rounded values; the output is uint8.
+def _addr(st):
+    return ctypes.addressof(st)
+
+
+def ref_render_scene(dims, origin, h, fields, temps, shape, cam, look, view, width, height):
+    L = ref_lib()
+    d, o, hh = _grid_args(dims, origin, h)
+    f = np.ascontiguousarray(fields, np.float32)
+    t = np.ascontiguousarray(temps, np.float32)
+    w = shape_words(shape)[:24].copy()
+    out = np.zeros((height, width, 4), np.float32)
+    L.wtr_render_scene(d.ctypes.data, o.ctypes.data, ctypes.c_float(hh), f.ctypes.data, t.ctypes.data, w.ctypes.data,
+                       _addr(cam), _addr(look), _addr(view), width, height, out.ctypes.data)
+    return out
+
+
+def ref_taa(cur, hist, taa):
+    L = ref_lib()
+    cur = np.ascontiguousarray(cur, np.float32)
+    hist = np.ascontiguousarray(hist, np.float32)
+    hgt, w = cur.shape[:2]
+    out = np.zeros_like(cur)
+    L.wtr_taa(cur.ctypes.data, hist.ctypes.data, w, hgt, _addr(taa), out.ctypes.data)
+    return out
+
+
+def ref_blur(src, dir_xy, spacing, gain, dw, dh):
+    L = ref_lib()
+    src = np.ascontiguousarray(src, np.float32)
+    b = np.array([dir_xy[0], dir_xy[1], spacing, gain], np.float32)
+    out = np.zeros((dh, dw, 4), np.float32)
+    L.wtr_blur(src.ctypes.data, src.shape[1], src.shape[0], b.ctypes.data, dw, dh, out.ctypes.data)
+    return out
+
+
+def ref_present(scene, glow, bloom, post):
+    L = ref_lib()
+    scene, glow, bloom = (np.ascontiguousarray(a, np.float32) for a in (scene, glow, bloom))
+    out = np.zeros(scene.shape, np.uint8)
+    L.wtr_present(scene.ctypes.data, scene.shape[1], scene.shape[0], glow.ctypes.data, glow.shape[1], glow.shape[0],
+                  bloom.ctypes.data, bloom.shape[1], bloom.shape[0], _addr(post), out.ctypes.data)
+    return out
+
+
+def ref_glow(scene, parts=None, pdraw=None, pts=None, sdraw=None):
+    """The glow pass: particle quads (2 * count instances) and streamline quads
+    (lines * 2 * (steps - 1) instances) added into a cleared target."""
+    L = ref_lib()
+    scene = np.ascontiguousarray(scene, np.float32)
+    hgt, w = scene.shape[:2]
+    out = np.zeros_like(scene)
+    pp = None if parts is None else np.ascontiguousarray(parts, np.float32)
+    sp = None if pts is None else np.ascontiguousarray(pts, np.float32)
+    n_p = 0 if pp is None else 2 * pdraw.count
+    n_s = 0 if sp is None else sdraw.lines * 2 * (sdraw.steps - 1)
+    L.wtr_glow(scene.ctypes.data, w, hgt, None if pp is None else pp.ctypes.data,
+               None if pp is None else _addr(pdraw), n_p, None if sp is None else sp.ctypes.data,
+               None if sp is None else _addr(sdraw), n_s, out.ctypes.data)
     return out
 
 

@@ -14,7 +14,10 @@
 #include "wgsl_runtime.hpp"
 #include "_ref/wgsl_modules.inc"
 
+#include <math.h>
 #include <stdlib.h>
+
+#include <algorithm>
 #include <string.h>
 #include <vector>
 #ifdef _OPENMP
@@ -41,6 +44,27 @@ void dispatch(uint32_t n, int nphases, F run) {
   for (int64_t wg = 0; wg < nwg; wg++)
     for (int ph = 0; ph < nphases; ph++)
       for (uint32_t li = 0; li < 128; li++) run(ph, rt::vec3u((uint32_t)(wg * 128 + li), 0u, 0u), li);
+}
+
+template <class S>
+void set_shape(S& s, const uint32_t* w) {
+  float f[24];
+  memcpy(f, w, sizeof(f));
+  s.kind = w[0]; s.profileMode = w[1]; s.pw = w[2]; s.ph = w[3];
+  s.frontFlap = f[4]; s.rearMain = f[5]; s.rearFlap = f[6]; s.rideH = f[7];
+  s.aoa = f[8]; s.width = f[9]; s.axisY = f[10]; s.pScale = f[11];
+  s.pOrigin = rt::vec2f(f[12], f[13]); s.heatBrakes = f[14]; s.heatEngine = f[15];
+  s.heatRad = f[16]; s.frontWing = f[17]; s.rearWing = f[18]; s.sidepod = f[19];
+  s.cover = f[20]; s.nose = f[21]; s.rearRide = f[22]; s.duct = f[23];
+}
+
+// Rig uniform as the engine creates it before any W17 model is loaded (engine.ts:273-277).
+template <class R>
+void set_rig(R& rig) {
+  rig = R{};
+  rig.extra = rt::vec4f(0.0f, 1.0f, 0.0f, 0.0f);
+  rig.fly = rt::vec4f(0.0f, 0.0f, 1.0f, 1.0f);
+  for (int i = 0; i < 12; i++) rig.grids[i] = rt::vec4f(0.0f, 0.0f, 0.0f, 1.0f);
 }
 
 template <class G>
@@ -125,20 +149,8 @@ void wtr_voxelize(void* p, const uint32_t* w) {
   Ref* r = (Ref*)p;
   namespace M = m_voxelize;
   set_grid(M::grid, *r);
-  float f[24];
-  memcpy(f, w, sizeof(f));
-  M::Shape& s = M::shape;
-  s.kind = w[0]; s.profileMode = w[1]; s.pw = w[2]; s.ph = w[3];
-  s.frontFlap = f[4]; s.rearMain = f[5]; s.rearFlap = f[6]; s.rideH = f[7];
-  s.aoa = f[8]; s.width = f[9]; s.axisY = f[10]; s.pScale = f[11];
-  s.pOrigin = rt::vec2f(f[12], f[13]); s.heatBrakes = f[14]; s.heatEngine = f[15];
-  s.heatRad = f[16]; s.frontWing = f[17]; s.rearWing = f[18]; s.sidepod = f[19];
-  s.cover = f[20]; s.nose = f[21]; s.rearRide = f[22]; s.duct = f[23];
-  // Rig uniform as the engine creates it before any W17 model is loaded (engine.ts:273-277).
-  M::rig = M::Rig{};
-  M::rig.extra = rt::vec4f(0.0f, 1.0f, 0.0f, 0.0f);
-  M::rig.fly = rt::vec4f(0.0f, 0.0f, 1.0f, 1.0f);
-  for (int i = 0; i < 12; i++) M::rig.grids[i] = rt::vec4f(0.0f, 0.0f, 0.0f, 1.0f);
+  set_shape(M::shape, w);
+  set_rig(M::rig);
   M::profile.p = r->profile.data();
   M::solid.p = r->solid.data();
   M::emit.p = r->emit.data();
@@ -261,6 +273,288 @@ void wtr_streamlines(const uint32_t* dims, const float* origin, float h, const f
   for (int i = 0; i < 8; i++) M::emitters.e[i] = rt::vec4f(emit[4 * i], emit[4 * i + 1], emit[4 * i + 2], emit[4 * i + 3]);
   set_view(M::view, view);
   dispatch(ss[0], M::cs_main_nphases, [](int ph, rt::vec3u gid, uint32_t li) { M::cs_main_run(ph, gid, li); });
+}
+
+// ---- render passes (src/engine/render-wgsl.ts; order and targets engine.ts:290-327, 714-725)
+//
+// Render targets are RGBA f32 arrays, row-major from the top row.  rgba16float
+// targets hold values rounded to binary16 (nearest, ties to even) on every
+// write, as the GPU stores them; the rgba8unorm output holds
+// round(clamp(x, 0, 1) * 255).  A full-screen pass invokes fs_main once per
+// texel of its target with uv = ((x + 0.5) / w, (y + 0.5) / h).
+extern "C++" {
+static float round_half(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  const uint32_t a = u & 0x7fffffffu;
+  const float sgn = (u >> 31) ? -1.0f : 1.0f;
+  if (a >= 0x7f800000u) return x;                     // inf, NaN
+  if (a >= 0x477ff000u) return sgn * __builtin_inff();  // >= 65520 rounds past 65504
+  if (a <= 0x33000000u) return sgn * 0.0f;            // <= 2^-25 rounds to zero
+  const int e = (int)(a >> 23) - 127;
+  const int q = e >= -14 ? e - 10 : -24;              // binary16 quantum at this magnitude
+  const float scale = __builtin_ldexpf(1.0f, q);
+  float ax;
+  memcpy(&ax, &a, 4);
+  return sgn * (__builtin_rintf(ax / scale) * scale);
+}
+static uint8_t unorm8(float x) {
+  if (!(x == x)) return 0;
+  const float c = x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x);
+  return (uint8_t)__builtin_rintf(c * 255.0f);
+}
+static rt::vec3f v3(const float* p) { return rt::vec3f(p[0], p[1], p[2]); }
+static rt::mat4x4f mat4(const float* m) {
+  rt::mat4x4f r;
+  for (int c = 0; c < 4; c++) r.c[c] = rt::vec4f(m[4 * c], m[4 * c + 1], m[4 * c + 2], m[4 * c + 3]);
+  return r;
+}
+template <class F>
+static void full_screen(int w, int h, F fs) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int y = 0; y < h; y++)
+    for (int x = 0; x < w; x++) {
+      const rt::vec2f uv(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+      fs(x, y, uv);
+    }
+}
+}  // extern "C++"
+
+// RENDER fs_main (render-wgsl.ts:288-398) into the rgba16float scene target.
+// shape: Shape words; cam: the Cam uniform (20 words: pos, tanHalf, fwd, aspect,
+// right, time, up, roadSpeed, jitter.xy, pad, pad); look: the Look uniform (24
+// words, render-wgsl.ts:12-19); view: View (8 floats).
+void wtr_render_scene(const uint32_t* dims, const float* origin, float h, const float* fields, const float* temps,
+                      const uint32_t* shape, const float* cam, const uint32_t* look, const float* view, int w,
+                      int hgt, float* scene) {
+  namespace M = m_render;
+  static std::vector<float> profile(256 * 128, 10.0f);  // engine.ts:245-246
+  set_grid_ext(M::grid, dims, origin, h);
+  M::fields.p = (rt::vec4f*)fields;
+  M::temps.p = (float*)temps;
+  M::profile.p = profile.data();
+  set_shape(M::shape, shape);
+  set_rig(M::rig);
+  M::cam.pos = v3(cam); M::cam.tanHalf = cam[3];
+  M::cam.fwd = v3(cam + 4); M::cam.aspect = cam[7];
+  M::cam.right = v3(cam + 8); M::cam.time = cam[11];
+  M::cam.up = v3(cam + 12); M::cam.roadSpeed = cam[15];
+  M::cam.jitter = rt::vec2f(cam[16], cam[17]); M::cam.pad0 = 0.0f; M::cam.pad1 = 0.0f;
+  float lf[24];
+  memcpy(lf, look, sizeof(lf));
+  M::Look& L = M::look;
+  L.bmin = v3(lf); L.surfMode = look[3];
+  L.bmax = v3(lf + 4); L.palette = look[7];
+  L.paint = v3(lf + 8); L.carbonBody = look[11];
+  L.accent = v3(lf + 12); L.isF1 = look[15];
+  L.sliceAxis = look[16]; L.slicePos = lf[17]; L.sliceAlpha = lf[18]; L.showFlow = look[19];
+  L.meshMode = look[20]; L.cooling = look[21]; L.pad1 = 0u; L.pad2 = 0u;
+  set_view(M::view, view);
+  full_screen(w, hgt, [&](int x, int y, rt::vec2f uv) {
+    const rt::vec4f c = M::fs_main(uv);
+    float* o = scene + ((size_t)y * w + x) * 4;
+    o[0] = round_half(c.x); o[1] = round_half(c.y); o[2] = round_half(c.z); o[3] = round_half(c.w);
+  });
+}
+
+// TAA fs_main (render-wgsl.ts:456-518): cur and hist are w x h rgba16float targets;
+// taa: the Taa uniform (32 floats: prevViewProj column-major, camPos, tanHalf,
+// fwd, aspect, right, blend, up, pad).
+void wtr_taa(const float* cur, const float* hist, int w, int hgt, const float* taa, float* out) {
+  namespace M = m_taa;
+  M::cur = rt::texture2d{w, hgt, cur};
+  M::hist = rt::texture2d{w, hgt, hist};
+  M::taa.prevViewProj = mat4(taa);
+  M::taa.camPos = v3(taa + 16); M::taa.tanHalf = taa[19];
+  M::taa.fwd = v3(taa + 20); M::taa.aspect = taa[23];
+  M::taa.right = v3(taa + 24); M::taa.blend = taa[27];
+  M::taa.up = v3(taa + 28); M::taa.pad = 0.0f;
+  full_screen(w, hgt, [&](int x, int y, rt::vec2f uv) {
+    const rt::vec4f c = M::fs_main(uv);
+    float* o = out + ((size_t)y * w + x) * 4;
+    o[0] = round_half(c.x); o[1] = round_half(c.y); o[2] = round_half(c.z); o[3] = round_half(c.w);
+  });
+}
+
+// BLUR fs_main (render-wgsl.ts:401-418) from an sw x sh source into a dw x dh
+// target; blur: dir.xy, spacing, gain.
+void wtr_blur(const float* src, int sw, int sh, const float* blur, int dw, int dh, float* out) {
+  namespace M = m_blur;
+  M::src = rt::texture2d{sw, sh, src};
+  M::blur.dir = rt::vec2f(blur[0], blur[1]); M::blur.spacing = blur[2]; M::blur.gain = blur[3];
+  full_screen(dw, dh, [&](int x, int y, rt::vec2f uv) {
+    const rt::vec4f c = M::fs_main(uv);
+    float* o = out + ((size_t)y * dw + x) * 4;
+    o[0] = round_half(c.x); o[1] = round_half(c.y); o[2] = round_half(c.z); o[3] = round_half(c.w);
+  });
+}
+
+// PRESENT fs_main (render-wgsl.ts:420-454) into the w x h rgba8unorm output:
+// scene (the resolved history), glow (gw x gh) and bloom (bw x bh) targets;
+// post: bloom, exposure, pad, pad.
+void wtr_present(const float* scene, int w, int hgt, const float* glow, int gw, int gh, const float* bloom, int bw,
+                 int bh, const float* post, uint8_t* out) {
+  namespace M = m_present;
+  M::scene = rt::texture2d{w, hgt, scene};
+  M::glow = rt::texture2d{gw, gh, glow};
+  M::bloomTex = rt::texture2d{bw, bh, bloom};
+  M::post.bloom = post[0]; M::post.exposure = post[1]; M::post.pad0 = 0.0f; M::post.pad1 = 0.0f;
+  full_screen(w, hgt, [&](int x, int y, rt::vec2f uv) {
+    const rt::vec4f c = M::fs_main(uv);
+    uint8_t* o = out + ((size_t)y * w + x) * 4;
+    o[0] = unorm8(c.x); o[1] = unorm8(c.y); o[2] = unorm8(c.z); o[3] = unorm8(c.w);
+  });
+}
+
+// ---- the glow pass: PARTICLES_DRAW (wgsl.ts:597-659) and STREAM_DRAW
+// (render-wgsl.ts:578-645) instanced quads, additively blended (one, one) into
+// the cleared rgba16float glow target (engine.ts:719-722).
+//
+// Fixed-function stages, as the WebGPU pipeline defines them, in the form both
+// this model and the device rasterizer evaluate:
+//   * triangle-list topology: vertices 0-2 and 3-5 of each instance;
+//   * clip -> NDC n = c.xyz / c.w; framebuffer X = (n.x * 0.5 + 0.5) * W,
+//     Y = (0.5 - n.y * 0.5) * H;
+//   * area A = (X1-X0)(Y2-Y0) - (X2-X0)(Y1-Y0); none or NaN -> no fragments;
+//   * pixel (px, py) is covered when its centre P = (px+0.5, py+0.5) gives edge
+//     values e0 = (X2-X1)(Py-Y1) - (Y2-Y1)(Px-X1), e1 = (X0-X2)(Py-Y2) - (Y0-Y2)(Px-X2),
+//     e2 = (X1-X0)(Py-Y0) - (Y1-Y0)(Px-X0), multiplied by sign(A), all >= 0,
+//     where an edge value of exactly 0 counts only for an edge whose direction
+//     (b - a, times sign(A)) has dy > 0, or dy == 0 and dx < 0 (so a pixel on an
+//     edge two triangles share is drawn once);
+//   * depth clip: z = b0 n0.z + b1 n1.z + b2 n2.z outside [0, 1] -> discarded;
+//   * perspective-correct varyings: with b_k = e_k / |A| and q_k = b_k / c_k.w,
+//     weight k = q_k / (q0 + q1 + q2), varying = w0 a0 + w1 a1 + w2 a2;
+//   * fragment position.xy = P.
+// Blending: the (one, one) sum is formed exactly, each fragment's value rounded
+// to a multiple of 2^-32 into 64-bit integers, and the total rounded once to
+// binary16 (the WebGPU blend unit's intermediate precision is the
+// implementation's; an exact sum makes the result independent of fragment order).
+extern "C++" {
+struct Vtx {
+  float X, Y, nz, iw;    // framebuffer position, NDC depth, 1 / clip w
+  float a[6];            // varyings: colour (4), side, dist
+};
+static bool raster_edge_owned(float dx, float dy) { return dy > 0.0f || (dy == 0.0f && dx < 0.0f); }
+template <class FS>
+static void raster_triangle(const Vtx* v, int W, int H, FS shade) {
+  const float A = (v[1].X - v[0].X) * (v[2].Y - v[0].Y) - (v[2].X - v[0].X) * (v[1].Y - v[0].Y);
+  if (!(A > 0.0f) && !(A < 0.0f)) return;
+  const float sg = A > 0.0f ? 1.0f : -1.0f;
+  const float aa = A > 0.0f ? A : -A;
+  const float minx = std::min(v[0].X, std::min(v[1].X, v[2].X)), maxx = std::max(v[0].X, std::max(v[1].X, v[2].X));
+  const float miny = std::min(v[0].Y, std::min(v[1].Y, v[2].Y)), maxy = std::max(v[0].Y, std::max(v[1].Y, v[2].Y));
+  const int x0 = (int)ceilf(std::min(std::max(minx - 0.5f, 0.0f), (float)W));
+  const int x1 = (int)floorf(std::max(std::min(maxx - 0.5f, (float)(W - 1)), -1.0f));
+  const int y0 = (int)ceilf(std::min(std::max(miny - 0.5f, 0.0f), (float)H));
+  const int y1 = (int)floorf(std::max(std::min(maxy - 0.5f, (float)(H - 1)), -1.0f));
+  const bool own0 = raster_edge_owned((v[2].X - v[1].X) * sg, (v[2].Y - v[1].Y) * sg);
+  const bool own1 = raster_edge_owned((v[0].X - v[2].X) * sg, (v[0].Y - v[2].Y) * sg);
+  const bool own2 = raster_edge_owned((v[1].X - v[0].X) * sg, (v[1].Y - v[0].Y) * sg);
+  for (int py = y0; py <= y1; py++)
+    for (int px = x0; px <= x1; px++) {
+      const float Px = (float)px + 0.5f, Py = (float)py + 0.5f;
+      const float e0 = ((v[2].X - v[1].X) * (Py - v[1].Y) - (v[2].Y - v[1].Y) * (Px - v[1].X)) * sg;
+      const float e1 = ((v[0].X - v[2].X) * (Py - v[2].Y) - (v[0].Y - v[2].Y) * (Px - v[2].X)) * sg;
+      const float e2 = ((v[1].X - v[0].X) * (Py - v[0].Y) - (v[1].Y - v[0].Y) * (Px - v[0].X)) * sg;
+      if (e0 < 0.0f || e1 < 0.0f || e2 < 0.0f) continue;
+      if ((e0 == 0.0f && !own0) || (e1 == 0.0f && !own1) || (e2 == 0.0f && !own2)) continue;
+      const float b0 = e0 / aa, b1 = e1 / aa, b2 = e2 / aa;
+      const float z = b0 * v[0].nz + b1 * v[1].nz + b2 * v[2].nz;
+      if (!(z >= 0.0f && z <= 1.0f)) continue;
+      const float q0 = b0 * v[0].iw, q1 = b1 * v[1].iw, q2 = b2 * v[2].iw;
+      const float qs = q0 + q1 + q2;
+      const float w0 = q0 / qs, w1 = q1 / qs, w2 = q2 / qs;
+      float a[6];
+      for (int k = 0; k < 6; k++) a[k] = w0 * v[0].a[k] + w1 * v[1].a[k] + w2 * v[2].a[k];
+      shade(px, py, Px, Py, z, a);
+    }
+}
+static Vtx make_vtx(rt::vec4f pos, int W, int H, const float* a) {
+  Vtx v;
+  const float nx = pos.x / pos.w, ny = pos.y / pos.w;
+  v.nz = pos.z / pos.w;
+  v.X = (nx * 0.5f + 0.5f) * (float)W;
+  v.Y = (0.5f - ny * 0.5f) * (float)H;
+  v.iw = 1.0f / pos.w;
+  for (int k = 0; k < 6; k++) v.a[k] = a[k];
+  return v;
+}
+static void accumulate(std::vector<int64_t>& acc, int W, int px, int py, rt::vec4f c) {
+  int64_t* o = acc.data() + ((size_t)py * W + px) * 4;
+  o[0] += llrint((double)c.x * 4294967296.0);
+  o[1] += llrint((double)c.y * 4294967296.0);
+  o[2] += llrint((double)c.z * 4294967296.0);
+  o[3] += llrint((double)c.w * 4294967296.0);
+}
+}  // extern "C++"
+
+// scene: the w x h rgba16float scene target (its alpha is the hit distance);
+// parts: count x 8 floats; pdraw: the PDraw uniform (28 words); n_pinst
+// instances (0 = no particle draw).  pts: lines x steps x 4 floats; sdraw: the
+// SDraw uniform (28 words); n_sinst instances (0 = no streamline draw).
+void wtr_glow(const float* scene, int w, int hgt, const float* parts, const uint32_t* pdraw, uint32_t n_pinst,
+              const float* pts, const uint32_t* sdraw, uint32_t n_sinst, float* glow) {
+  std::vector<int64_t> acc((size_t)w * hgt * 4, 0);
+  if (n_pinst) {
+    namespace M = m_pdraw;
+    float f[28];
+    memcpy(f, pdraw, sizeof(f));
+    M::pd.viewProj = mat4(f); M::pd.camPos = v3(f + 16); M::pd.width = f[19];
+    M::pd.res = rt::vec2f(f[20], f[21]); M::pd.trail = f[22]; M::pd.alpha = f[23];
+    M::pd.count = pdraw[24]; M::pd.palette = pdraw[25]; M::pd.fadeIn = f[26]; M::pd.pad = 0.0f;
+    M::parts.p = (M::Particle*)parts;
+    M::scene = rt::texture2d{w, hgt, scene};
+    for (uint32_t ii = 0; ii < n_pinst; ii++)
+      for (int t = 0; t < 2; t++) {
+        Vtx v[3];
+        for (int k = 0; k < 3; k++) {
+          const M::VOut o = M::vs_main((uint32_t)(3 * t + k), ii);
+          const float a[6] = {o.color.x, o.color.y, o.color.z, o.color.w, o.side, o.dist};
+          v[k] = make_vtx(o.pos, w, hgt, a);
+        }
+        raster_triangle(v, w, hgt, [&](int px, int py, float Px, float Py, float z, const float* a) {
+          M::VOut in{};
+          in.pos = rt::vec4f(Px, Py, z, 1.0f);
+          in.color = rt::vec4f(a[0], a[1], a[2], a[3]);
+          in.side = a[4];
+          in.dist = a[5];
+          M::rt_discarded = false;
+          const rt::vec4f c = M::fs_main(in);
+          if (!M::rt_discarded) accumulate(acc, w, px, py, c);
+        });
+      }
+  }
+  if (n_sinst) {
+    namespace M = m_sdraw;
+    float f[28];
+    memcpy(f, sdraw, sizeof(f));
+    M::sd.viewProj = mat4(f); M::sd.camPos = v3(f + 16); M::sd.width = f[19];
+    M::sd.res = rt::vec2f(f[20], f[21]); M::sd.time = f[22]; M::sd.intensity = f[23];
+    M::sd.lines = sdraw[24]; M::sd.steps = sdraw[25]; M::sd.palette = sdraw[26]; M::sd.pulse = f[27];
+    M::pts.p = (rt::vec4f*)pts;
+    M::scene = rt::texture2d{w, hgt, scene};
+    for (uint32_t ii = 0; ii < n_sinst; ii++)
+      for (int t = 0; t < 2; t++) {
+        Vtx v[3];
+        for (int k = 0; k < 3; k++) {
+          const M::VOut o = M::vs_main((uint32_t)(3 * t + k), ii);
+          const float a[6] = {o.color.x, o.color.y, o.color.z, 0.0f, o.side, o.dist};
+          v[k] = make_vtx(o.pos, w, hgt, a);
+        }
+        raster_triangle(v, w, hgt, [&](int px, int py, float Px, float Py, float z, const float* a) {
+          M::VOut in{};
+          in.pos = rt::vec4f(Px, Py, z, 1.0f);
+          in.color = rt::vec3f(a[0], a[1], a[2]);
+          in.side = a[4];
+          in.dist = a[5];
+          M::rt_discarded = false;
+          const rt::vec4f c = M::fs_main(in);
+          if (!M::rt_discarded) accumulate(acc, w, px, py, c);
+        });
+      }
+  }
+  for (size_t i = 0; i < acc.size(); i++) glow[i] = round_half((float)((double)acc[i] * 0x1p-32));
 }
 
 int wtr_threads(void) {

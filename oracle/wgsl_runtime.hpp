@@ -55,6 +55,7 @@ template <class T> struct conv;
 template <> struct conv<f32> { template <class S> static f32 c(S s) { return to_f32(s); } };
 template <> struct conv<i32> { template <class S> static i32 c(S s) { return to_i32(s); } };
 template <> struct conv<u32> { template <class S> static u32 c(S s) { return to_u32(s); } };
+template <> struct conv<bool> { template <class S> static bool c(S s) { return (bool)s; } };
 // abstract-int literals (C++ int) and other arithmetic types
 template <class T, class S> static inline T cv(S s) { return conv<T>::c(s); }
 template <> inline f32 cv<f32, double>(double s) { return (f32)s; }
@@ -64,6 +65,14 @@ template <class T> struct vec2;
 template <class T> struct vec3;
 template <class T> struct vec4;
 
+// v.swz<i, j, ...>() builds a vector from components i, j, ... (WGSL swizzles).
+#define RT_SWIZZLES                                                                                \
+  template <int A, int B> vec2<T> swz() const { return vec2<T>((*this)[A], (*this)[B]); }            \
+  template <int A, int B, int C> vec3<T> swz() const { return vec3<T>((*this)[A], (*this)[B], (*this)[C]); } \
+  template <int A, int B, int C, int D> vec4<T> swz() const {                                       \
+    return vec4<T>((*this)[A], (*this)[B], (*this)[C], (*this)[D]);                                  \
+  }
+
 template <class T> struct vec2 {
   T x, y;
   vec2() : x(0), y(0) {}
@@ -72,6 +81,9 @@ template <class T> struct vec2 {
   template <class S> vec2(const vec2<S>& v) : x(cv<T>(v.x)), y(cv<T>(v.y)) {}
   vec2(const vec2& v) = default;
   vec2& operator=(const vec2& v) = default;
+  T& operator[](int64_t i) { return i == 0 ? x : y; }
+  T operator[](int64_t i) const { return i == 0 ? x : y; }
+  RT_SWIZZLES
 };
 template <class T> struct vec3 {
   T x, y, z;
@@ -84,6 +96,9 @@ template <class T> struct vec3 {
   vec3& operator=(const vec3& v) = default;
   vec2<T> xy() const { return vec2<T>(x, y); }
   vec2<T> yz() const { return vec2<T>(y, z); }
+  T& operator[](int64_t i) { return i == 0 ? x : (i == 1 ? y : z); }
+  T operator[](int64_t i) const { return i == 0 ? x : (i == 1 ? y : z); }
+  RT_SWIZZLES
 };
 template <class T> struct vec4 {
   T x, y, z, w;
@@ -92,12 +107,17 @@ template <class T> struct vec4 {
   template <class A, class B, class C, class D>
   vec4(A a, B b, C c, D d) : x(cv<T>(a)), y(cv<T>(b)), z(cv<T>(c)), w(cv<T>(d)) {}
   template <class S, class D> vec4(const vec3<S>& v, D d) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(v.z)), w(cv<T>(d)) {}
+  template <class S, class C, class D>
+  vec4(const vec2<S>& v, C c, D d) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(c)), w(cv<T>(d)) {}
   template <class S> vec4(const vec4<S>& v) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(v.z)), w(cv<T>(v.w)) {}
   vec4(const vec4& v) = default;
   vec4& operator=(const vec4& v) = default;
   vec2<T> xy() const { return vec2<T>(x, y); }
   vec2<T> zw() const { return vec2<T>(z, w); }
   vec3<T> xyz() const { return vec3<T>(x, y, z); }
+  T& operator[](int64_t i) { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+  T operator[](int64_t i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+  RT_SWIZZLES
 };
 typedef vec2<f32> vec2f; typedef vec3<f32> vec3f; typedef vec4<f32> vec4f;
 typedef vec2<i32> vec2i; typedef vec3<i32> vec3i; typedef vec4<i32> vec4i;
@@ -125,6 +145,31 @@ template <class T> vec2<T> operator-(const vec2<T>& a) { return vec2<T>(-a.x, -a
 template <class T> vec3<T> operator-(const vec3<T>& a) { return vec3<T>(-a.x, -a.y, -a.z); }
 template <class T> vec4<T> operator-(const vec4<T>& a) { return vec4<T>(-a.x, -a.y, -a.z, -a.w); }
 
+// Component-wise comparisons give bool vectors (WGSL), reduced by all()/any().
+#define RT_VCMP(OP)                                                                                \
+  template <class T> vec2<bool> operator OP(const vec2<T>& a, const vec2<T>& b) { return vec2<bool>(a.x OP b.x, a.y OP b.y); } \
+  template <class T> vec3<bool> operator OP(const vec3<T>& a, const vec3<T>& b) { return vec3<bool>(a.x OP b.x, a.y OP b.y, a.z OP b.z); }
+RT_VCMP(<)
+RT_VCMP(<=)
+RT_VCMP(>)
+RT_VCMP(>=)
+#undef RT_VCMP
+static inline bool all(const vec2<bool>& v) { return v.x && v.y; }
+static inline bool all(const vec3<bool>& v) { return v.x && v.y && v.z; }
+
+// mat4x4f: four columns; m * v = c0 v.x + c1 v.y + c2 v.z + c3 v.w, summed in that order.
+struct mat4x4f {
+  vec4<f32> c[4];
+};
+static inline vec4<f32> operator*(const mat4x4f& m, const vec4<f32>& v) {
+  vec4<f32> r;
+  r.x = m.c[0].x * v.x + m.c[1].x * v.y + m.c[2].x * v.z + m.c[3].x * v.w;
+  r.y = m.c[0].y * v.x + m.c[1].y * v.y + m.c[2].y * v.z + m.c[3].y * v.w;
+  r.z = m.c[0].z * v.x + m.c[1].z * v.y + m.c[2].z * v.z + m.c[3].z * v.w;
+  r.w = m.c[0].w * v.x + m.c[1].w * v.y + m.c[2].w * v.z + m.c[3].w * v.w;
+  return r;
+}
+
 // ---- fixed-size arrays ---------------------------------------------------
 template <class T, int N> struct array {
   T a[N];
@@ -147,6 +192,18 @@ struct sampler { int dummy = 0; };
 // Textures only feed the baked-mesh (W17) scene, which this model does not evaluate.
 static inline vec4f textureSampleLevel(const texture3d&, const sampler&, vec3f, f32) { return vec4f(0.0f); }
 static inline vec3u textureDimensions(const texture3d&) { return vec3u(1u, 1u, 1u); }
+// A 2-D render target read by textureLoad: w x h texels of RGBA f32 (already
+// rounded to the target format by whoever wrote it).
+struct texture2d {
+  int w = 1, h = 1;
+  const f32* p = nullptr;
+};
+static inline vec2u textureDimensions(const texture2d& t) { return vec2u((u32)t.w, (u32)t.h); }
+static inline vec4f textureLoad(const texture2d& t, vec2i q, i32) {
+  if (!t.p || q.x < 0 || q.y < 0 || q.x >= t.w || q.y >= t.h) return vec4f(0.0f);
+  const f32* e = t.p + ((size_t)q.y * (size_t)t.w + (size_t)q.x) * 4;
+  return vec4f(e[0], e[1], e[2], e[3]);
+}
 
 // ---- builtins -----------------------------------------------------------
 static inline f32 abs(f32 x) { return x < 0.0f ? -x : (x == 0.0f ? 0.0f : x); }
@@ -169,6 +226,7 @@ template <class T> T clamp(const T& e, const T& lo, const T& hi) { return min(ma
 static inline f32 mix(f32 a, f32 b, f32 t) { return a * (1.0f - t) + b * t; }
 template <class T> vec2<T> mix(const vec2<T>& a, const vec2<T>& b, f32 t) { return vec2<T>(mix(a.x, b.x, t), mix(a.y, b.y, t)); }
 template <class T> vec3<T> mix(const vec3<T>& a, const vec3<T>& b, f32 t) { return vec3<T>(mix(a.x, b.x, t), mix(a.y, b.y, t), mix(a.z, b.z, t)); }
+template <class T> vec4<T> mix(const vec4<T>& a, const vec4<T>& b, f32 t) { return vec4<T>(mix(a.x, b.x, t), mix(a.y, b.y, t), mix(a.z, b.z, t), mix(a.w, b.w, t)); }
 static inline f32 smoothstep(f32 lo, f32 hi, f32 x) {
   f32 t = clamp((x - lo) / (hi - lo), 0.0f, 1.0f);
   return t * t * (3.0f - 2.0f * t);
@@ -184,6 +242,19 @@ static inline f32 sign(f32 x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0
 static inline f32 sin(f32 x) { return wtm::sinf(x); }
 static inline f32 cos(f32 x) { return wtm::cosf(x); }
 static inline f32 atan(f32 x) { return wtm::atanf(x); }
+static inline f32 atan2(f32 y, f32 x) { return wtm::atan2f(y, x); }
+static inline f32 exp(f32 x) { return wtm::expf(x); }
+static inline f32 exp2(f32 x) { return wtm::exp2f(x); }
+static inline f32 log2(f32 x) { return wtm::log2f(x); }
+static inline f32 pow(f32 x, f32 y) { return wtm::powf(x, y); }
+static inline vec3f pow(const vec3f& x, const vec3f& y) { return vec3f(pow(x.x, y.x), pow(x.y, y.y), pow(x.z, y.z)); }
+static inline vec3f sqrt(const vec3f& v) { return vec3f(sqrt(v.x), sqrt(v.y), sqrt(v.z)); }
+// fract(e) = e - floor(e)
+static inline f32 fract(f32 x) { return x - floor(x); }
+static inline vec2f fract(const vec2f& v) { return vec2f(fract(v.x), fract(v.y)); }
+static inline vec3f fract(const vec3f& v) { return vec3f(fract(v.x), fract(v.y), fract(v.z)); }
+// step(edge, x) = 1 if edge <= x else 0
+static inline f32 step(f32 edge, f32 x) { return edge <= x ? 1.0f : 0.0f; }
 
 static inline f32 dot(const vec2f& a, const vec2f& b) { return a.x * b.x + a.y * b.y; }
 static inline f32 dot(const vec3f& a, const vec3f& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
@@ -192,6 +263,9 @@ static inline f32 length(f32 x) { return abs(x); }
 template <class V> static inline f32 length(const V& v) { return sqrt(dot(v, v)); }
 // normalize(e) = e / length(e), one IEEE division per component
 template <class V> static inline V normalize(const V& v) { return v / length(v); }
+// reflect(e1, e2) = e1 - 2 dot(e2, e1) e2;  distance(a, b) = length(a - b)
+static inline vec3f reflect(const vec3f& e1, const vec3f& e2) { return e1 - (2.0f * dot(e2, e1)) * e2; }
+template <class V> static inline f32 distance(const V& a, const V& b) { return length(a - b); }
 
 template <class T> static inline T bitcast(f32 x) { T r; memcpy(&r, &x, 4); return r; }
 
@@ -210,4 +284,7 @@ template <class T> static inline T atomicLoad(T* p) { return __atomic_load_n(p, 
   using rt::clamp; using rt::mix; using rt::smoothstep; using rt::select; using rt::sqrt;            \
   using rt::floor; using rt::normalize; using rt::round; using rt::sign; using rt::sin; using rt::cos; using rt::atan;    \
   using rt::dot; using rt::length; using rt::bitcast; using rt::atomicAdd; using rt::atomicStore;   \
-  using rt::atomicLoad; using rt::textureSampleLevel; using rt::textureDimensions;
+  using rt::atomicLoad; using rt::textureSampleLevel; using rt::textureDimensions;                 \
+  using rt::texture2d; using rt::textureLoad; using rt::mat4x4f; using rt::all; using rt::atan2;    \
+  using rt::exp; using rt::exp2; using rt::log2; using rt::pow; using rt::fract; using rt::step;     \
+  using rt::reflect; using rt::distance;

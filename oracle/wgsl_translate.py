@@ -204,6 +204,8 @@ def cxx_type(t):
         return f"{cxx_type(m.group(1))}*"
     if t == "texture_3d<f32>":
         return "texture3d"
+    if t == "texture_2d<f32>":
+        return "texture2d"
     return t
 
 
@@ -224,7 +226,14 @@ def translate_module(name, wgsl, report):
     code = fold_abstract(code, report)
     code = suffix_floats(code)
     code = re.sub(r"\b(i32|u32|f32)\(", r"to_\1(", code)
-    code = re.sub(r"\.([xyzw]{2,4})\b", r".\1()", code)
+    code = re.sub(r"\.([xyzw]{2,4}|[rgba]{2,4})\b", swizzle, code)
+    code = re.sub(r"\.([rgba])\b", lambda m: "." + "xyzw"["rgba".index(m.group(1))], code)
+    # render-pipeline entry points become plain functions the driver calls per
+    # pixel / per vertex; interface attributes carry no arithmetic
+    code = re.sub(r"@(fragment|vertex)\s*", "", code)
+    code = re.sub(r"@location\(\d+\)\s*", "", code)
+    code = re.sub(r"@interpolate\([^)]*\)\s*", "", code)
+    struct_names = re.findall(r"\bstruct\s+(\w+)", code)
 
     structs, globs, protos, funcs = [], [], [], []
     entry = None
@@ -246,6 +255,7 @@ def translate_module(name, wgsl, report):
             fields = []
             for ln in body.split("\n"):
                 ln = re.sub(r"//.*", "", ln)
+                ln = re.sub(r"@builtin\(\w+\)\s*", "", ln)
                 for f in split_top(ln):
                     if ":" in f:
                         fn, ft = f.split(":", 1)
@@ -318,11 +328,18 @@ def translate_module(name, wgsl, report):
             else:
                 sig = f"static {ret} {fname}({', '.join(params)})"
                 protos.append(sig + ";")
-                funcs.append(sig + " {" + stmt_rewrite(ordered_constructors(body)) + "}")
+                body = brace_structs(ordered_constructors(body), struct_names)
+                body = re.sub(r"\bdiscard\s*;", "{ rt_discarded = true; return {}; }", body)
+                funcs.append(sig + " {" + stmt_rewrite(body) + "}")
             i = k
             continue
         raise SystemExit(f"{name}: cannot parse near: {code[i:i+80]!r}")
 
+    if "rt_discarded" in "".join(funcs):
+        globs.append("static thread_local bool rt_discarded = false;")
+    if entry is None:  # render module: fs_main / vs_main are called directly
+        return "\n".join([f"namespace {name} {{", "RT_USING", *structs, *globs, *protos, *funcs,
+                          f"}}  // namespace {name}", ""])
     params, builtins, body = entry
     phases = re.split(r"\bworkgroupBarrier\(\)\s*;", body)
     ent = []
@@ -339,6 +356,32 @@ def translate_module(name, wgsl, report):
     ent.append("}")
     return "\n".join([f"namespace {name} {{", "RT_USING", *structs, *globs, *protos, *funcs, *ent,
                       f"}}  // namespace {name}", ""])
+
+
+def swizzle(m):
+    """v.xzy / v.rgb -> v.swz<0,2,1>() (a member template of the runtime's vectors)."""
+    letters = m.group(1)
+    names = "xyzw" if letters[0] in "xyzw" else "rgba"
+    return ".swz<" + ",".join(str(names.index(c)) for c in letters) + ">()"
+
+
+def brace_structs(s, names):
+    """Struct constructors Name(a, b, ...) -> Name{a, b, ...}: aggregate
+    initialisation, whose initialisers C++ evaluates left to right as WGSL does."""
+    if not names:
+        return s
+    out, i = [], 0
+    for m in re.finditer(r"\b(" + "|".join(names) + r")\(", s):
+        if m.start() < i:
+            continue
+        depth, j = 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(s[j], 0)
+            j += 1
+        out.append(s[i:m.start()] + m.group(1) + "{" + brace_structs(s[m.end():j - 1], names) + "}")
+        i = j
+    out.append(s[i:])
+    return "".join(out)
 
 
 def ordered_constructors(s):
@@ -405,6 +448,12 @@ def main():
         "m_heat": "HEAT",
         "m_particles": "PARTICLES_SIM",
         "m_stream": "STREAM_SIM",
+        "m_render": "RENDER",
+        "m_blur": "BLUR",
+        "m_present": "PRESENT",
+        "m_taa": "TAA",
+        "m_pdraw": "PARTICLES_DRAW",
+        "m_sdraw": "STREAM_DRAW",
     }
     os.makedirs(OUT, exist_ok=True)
     chunks = [

@@ -1,0 +1,117 @@
+#!/usr/bin/env python3
+"""Generate the render fixture (render.npz) from the reference itself.
+
+The reference's own render shaders (src/engine/render-wgsl.ts RENDER, TAA,
+BLUR, PRESENT, STREAM_DRAW and src/engine/wgsl.ts PARTICLES_DRAW), translated
+to C++ by oracle/wgsl_translate.py and built by oracle/Makefile `ref`, run in
+the engine's pass order (engine.ts:714-725) over the flow of the consumer
+fixture (consumers.npz: the generic F1 on a 64x24x20 lattice, its particles
+after five passes and its streamlines).  The fixed-function stages (viewport,
+rasterization, blending) are the oracle's restatement of the WebGPU pipeline
+(oracle/ref_driver.cpp).
+
+Five sequences of frames at 128x72 cover the scene pass's branches:
+  hero      livery, ground reflection and belt, streamline glow; then a second
+            frame from a slightly moved camera, which reprojects the history
+  surface   pressure colour on the body surface (surfMode 1, palette 1)
+  slice-z   z slice with temperature colours, particle glow (palette 2)
+  slice-x   x slice with vorticity colours, vortex streamlines (palette 3)
+  slice-y   y slice with the wake map (palette 4), a carbon-free paint livery
+Stored per frame: the scene, resolved history, glow and bloom B targets
+(binary16) and the presented RGBA8 output.
+
+Needs the reference checkout (build container only); the fixture travels with
+the repository so the GPU kernels are pinned anywhere.
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "f1-wind-tunnel_gb300"))
+sys.path.insert(0, HERE)
+
+import make_consumers as mc  # noqa: E402
+from windtunnel import render as R  # noqa: E402
+from windtunnel.engine import ShapeKind  # noqa: E402
+from windtunnel.workloads import config_f1_shape  # noqa: E402
+
+OUT = os.path.join(HERE, "render.npz")
+W, H = 128, 72
+SHAPE_SEED = 3  # the consumer fixture's car
+
+
+class _Params:
+    """The shape fields make_look reads."""
+    kind = ShapeKind.F1
+
+    def __init__(self, shape):
+        self.ride_h = shape.ride_h
+
+
+def sequences(z):
+    """[(name, [frame dict, ...]), ...]; each frame: camera, look, glow inputs."""
+    shape = config_f1_shape(SHAPE_SEED)
+    p = _Params(shape)
+    parts = z["particles"][-1]
+    asp = W / H
+    hero = dict(cam=R.orbit_camera((2.75, 0.42, 0.0), 2.3, 0.3, 7.6, asp), look=R.make_look(p, palette=0),
+                lines=z["lines_rake"], color_mode=0, flow_time=0.7)
+    hero2 = dict(hero, cam=R.orbit_camera((2.75, 0.42, 0.0), 2.33, 0.29, 7.5, asp))
+    surface = dict(cam=R.orbit_camera((2.4, 0.5, 0.0), math.pi + 0.001, 0.12, 5.0, asp),
+                   look=R.make_look(p, palette=1, surface_field=True))
+    slice_z = dict(cam=R.orbit_camera((2.0, 0.6, 0.0), 1.9, 0.35, 7.0, asp),
+                   look=R.make_look(p, palette=2, slice_axis=3, slice_pos=0.35), parts=parts, color_mode=2, smoke=True)
+    slice_x = dict(cam=R.orbit_camera((3.0, 0.5, 0.3), 2.7, 0.2, 6.0, asp),
+                   look=R.make_look(p, palette=3, slice_axis=1, slice_pos=3.2), lines=z["lines_ring"], color_mode=3,
+                   flow_time=1.3, vortices=True)
+    slice_y = dict(cam=R.orbit_camera((2.5, 0.4, 0.0), 0.6, 0.5, 6.5, asp),
+                   look=R.make_look(p, palette=4, slice_axis=2, slice_pos=0.3, paint=(0.7, 0.1, 0.1), carbon=False),
+                   parts=parts, color_mode=4, smoke=False)
+    return shape, [("hero", [hero, hero2]), ("surface", [surface]), ("slice-z", [slice_z]), ("slice-x", [slice_x]),
+                   ("slice-y", [slice_y])]
+
+
+def frame_uniforms(state, f):
+    return state.next(f["cam"], (W, H), parts=f.get("parts"), color_mode=f.get("color_mode", 0),
+                      smoke=f.get("smoke", True), lines=f.get("lines"), flow_time=f.get("flow_time", 0.0),
+                      vortices=f.get("vortices", False))
+
+
+def main():
+    from oracle import pyoracle
+    z = np.load(os.path.join(HERE, "consumers.npz"))
+    shape, seqs = sequences(z)
+    view = mc.view()
+    hw, hh = W // 2, H // 2
+    out = {}
+    for name, frames in seqs:
+        st = R.FrameState()
+        hist = [np.zeros((H, W, 4), np.float32), np.zeros((H, W, 4), np.float32)]
+        for k, f in enumerate(frames):
+            u = frame_uniforms(st, f)
+            scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, z["fields"], z["temps"], shape, u.cam, f["look"],
+                                              view, W, H)
+            hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)
+            glow = pyoracle.ref_glow(scene, f.get("parts"), u.pdraw, f.get("lines"), u.sdraw)
+            ba = pyoracle.ref_blur(glow, (1.0, 0.0), 3.0, 1.0, hw, hh)
+            bb = pyoracle.ref_blur(ba, (0.0, 1.0), 1.5, 1.0, hw, hh)
+            rgba = pyoracle.ref_present(hist[u.cur], glow, bb, u.post)
+            key = f"{name}_{k}"
+            out[key + "_scene"] = scene.astype(np.float16)
+            out[key + "_hist"] = hist[u.cur].astype(np.float16)
+            out[key + "_glow"] = glow.astype(np.float16)
+            out[key + "_bloom"] = bb.astype(np.float16)
+            out[key + "_out"] = rgba
+            print(key, "hit pixels", int((scene[..., 3] < 6e4).sum()), "glow pixels", int((glow[..., 3] > 0).sum()),
+                  "mean rgb", rgba[..., :3].mean().round(2))
+    np.savez_compressed(OUT, **out)
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    main()

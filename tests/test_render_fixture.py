@@ -1,0 +1,90 @@
+"""The render fixture (tests/golden/render.npz) against the reference's own
+render shaders: where the translated reference is built (the build
+container), rerunning the frames reproduces every target bit for bit;
+everywhere, the fixture is self-consistent.  Also the host-side camera and
+jitter helpers against camera.ts / engine.ts semantics."""
+import math
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, GOLDEN)
+sys.path.insert(0, os.path.join(ROOT, "f1-wind-tunnel_gb300"))
+
+TARGETS = ("scene", "hist", "glow", "bloom", "out")
+
+
+def fixture():
+    return np.load(os.path.join(GOLDEN, "render.npz"))
+
+
+def test_fixture_is_consistent():
+    import make_render as mr
+    z = fixture()
+    keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
+    assert keys == ["hero_0", "hero_1", "slice-x_0", "slice-y_0", "slice-z_0", "surface_0"]
+    for k in keys:
+        sc, out = z[k + "_scene"].astype(np.float32), z[k + "_out"]
+        assert sc.shape == (mr.H, mr.W, 4) and out.shape == (mr.H, mr.W, 4) and out.dtype == np.uint8
+        assert z[k + "_bloom"].shape == (mr.H // 2, mr.W // 2, 4)
+        assert np.isfinite(sc).all() and (sc[..., 3] > 0).all() and (sc[..., 3] <= 6e4).all()
+        assert (out[..., 3] == 255).all()
+        assert (z[k + "_glow"].astype(np.float32) >= 0).all()
+    # the car is in view, the glow draws hit pixels, history reprojection changed the second frame
+    assert (z["hero_0_scene"][..., 3].astype(np.float32) < 20).sum() > 1000
+    assert (z["hero_0_glow"][..., 3] > 0).sum() > 500 and (z["slice-z_0_glow"][..., 3] > 0).sum() > 50
+    assert not np.array_equal(z["hero_1_hist"], z["hero_1_scene"])
+
+
+def test_reference_reproduces_fixture():
+    from oracle import pyoracle
+    if pyoracle.ref_lib() is None:
+        pytest.skip("translated reference not built (needs the reference checkout)")
+    import make_consumers as mc
+    import make_render as mr
+    from windtunnel import render as R
+    z = fixture()
+    c = np.load(os.path.join(GOLDEN, "consumers.npz"))
+    shape, seqs = mr.sequences(c)
+    for name, frames in seqs:
+        st = R.FrameState()
+        hist = [np.zeros((mr.H, mr.W, 4), np.float32) for _ in range(2)]
+        for k, f in enumerate(frames):
+            u = mr.frame_uniforms(st, f)
+            scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, c["fields"], c["temps"], shape, u.cam,
+                                              f["look"], mc.view(), mr.W, mr.H)
+            hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)
+            glow = pyoracle.ref_glow(scene, f.get("parts"), u.pdraw, f.get("lines"), u.sdraw)
+            bb = pyoracle.ref_blur(pyoracle.ref_blur(glow, (1.0, 0.0), 3.0, 1.0, mr.W // 2, mr.H // 2), (0.0, 1.0),
+                                   1.5, 1.0, mr.W // 2, mr.H // 2)
+            out = pyoracle.ref_present(hist[u.cur], glow, bb, u.post)
+            key = f"{name}_{k}"
+            for t, v in zip(TARGETS, (scene, hist[u.cur], glow, bb)):
+                assert np.array_equal(v.astype(np.float16).view(np.uint16), z[f"{key}_{t}"].view(np.uint16)), (key, t)
+            assert np.array_equal(out, z[key + "_out"]), key
+
+
+def test_orbit_camera_and_jitter():
+    from windtunnel import render as R
+    cam = R.orbit_camera((2.75, 0.42, 0.0), 2.3, 0.3, 7.6, 16 / 9)
+    assert abs(math.dist(cam.pos, (2.75, 0.42, 0.0)) - 7.6) < 1e-12
+    for v in (cam.fwd, cam.right, cam.up):
+        assert abs(math.hypot(*v) - 1.0) < 1e-12
+    assert abs(sum(a * b for a, b in zip(cam.fwd, cam.right))) < 1e-12
+    # the orbit target projects to the centre of the view, in front of the camera
+    m = cam.view_proj.reshape(4, 4).T.astype(np.float64)
+    clip = m @ np.array([2.75, 0.42, 0.0, 1.0])
+    assert clip[3] > 0 and abs(clip[0] / clip[3]) < 1e-5 and abs(clip[1] / clip[3]) < 1e-5
+    assert 0.0 < clip[2] / clip[3] < 1.0
+    assert [R.halton(i, 2) for i in (1, 2, 3, 4)] == [0.5, 0.25, 0.75, 0.125]
+    assert abs(R.halton(1, 3) - 1 / 3) < 1e-15 and abs(R.halton(5, 3) - 7 / 9) < 1e-15
+    st = R.FrameState()
+    a = st.next(cam, (128, 72))
+    b = st.next(cam, (128, 72))
+    assert (a.cur, b.cur) == (1, 0) and a.taa.blend == 1.0 and abs(b.taa.blend - 0.1) < 1e-7
+    assert abs(a.cam.jitter[0] - (R.halton(2, 2) - 0.5) * 2 / 128) < 1e-7
