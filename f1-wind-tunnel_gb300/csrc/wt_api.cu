@@ -18,6 +18,11 @@
 
 using namespace wt;
 
+struct wt_renderer;
+namespace {
+void release_renderer_buffers(wt_renderer* r);
+}
+
 struct wt_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -76,6 +81,7 @@ struct wt_ctx {
   };
   std::vector<Graph> graphs;               // captured wt_step sequences
   wt_shape shape{WT_KIND_EMPTY};           // last voxelized shape (the renderer's scene)
+  std::vector<wt_renderer*> renderers;     // live renderers over this lattice
   std::string err;
 };
 
@@ -489,6 +495,10 @@ int wt_destroy(wt_ctx* c) {
   if (!c) return WT_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  // Renderers still open over this lattice lose their targets here; a later
+  // wt_render_destroy only frees the handle, and other calls on it fail.
+  for (wt_renderer* r : c->renderers) release_renderer_buffers(r);
+  c->renderers.clear();
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
                   c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters,
@@ -1240,8 +1250,19 @@ F3 f3n(float x, float y, float z) {  // normalize(e) = e / length(e), IEEE opera
   return F3{x / l, y / l, z / l};
 }
 int render_check(wt_renderer* r) {
-  if (!r || !r->c) return WT_ERR_ARG;
+  if (!r || !r->c) return WT_ERR_ARG;  // also: its context was destroyed
   return check_ctx(r->c);
+}
+void release_renderer_buffers(wt_renderer* r) {
+  void* bufs[] = {r->scene, r->hist[0], r->hist[1], r->glow, r->bloom_a, r->bloom_b, r->out, r->acc, r->staging};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  r->scene = r->hist[0] = r->hist[1] = r->glow = r->bloom_a = r->bloom_b = nullptr;
+  r->out = nullptr;
+  r->acc = nullptr;
+  r->staging = nullptr;
+  r->staging_bytes = 0;
+  r->c = nullptr;
 }
 void* target_ptr(wt_renderer* r, int t, size_t* bytes) {
   const size_t full = (size_t)r->w * r->h, half = (size_t)r->hw * r->hh;
@@ -1272,10 +1293,16 @@ int draw_source(wt_renderer* r, const float* p, int on_device, size_t bytes, siz
 
 void wt_render_destroy(wt_renderer* r) {
   if (!r) return;
-  if (r->c) cudaStreamSynchronize(r->c->stream);
-  void* bufs[] = {r->scene, r->hist[0], r->hist[1], r->glow, r->bloom_a, r->bloom_b, r->out, r->acc, r->staging};
-  for (void* b : bufs)
-    if (b) cudaFree(b);
+  if (wt_ctx* c = r->c) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (size_t i = 0; i < c->renderers.size(); i++)
+      if (c->renderers[i] == r) {
+        c->renderers.erase(c->renderers.begin() + (long)i);
+        break;
+      }
+    release_renderer_buffers(r);
+  }
   delete r;
 }
 
@@ -1307,10 +1334,12 @@ int wt_render_create(wt_ctx* c, uint32_t width, uint32_t height, wt_renderer** o
   alloc((void**)&r->out, full * 4);
   alloc((void**)&r->acc, full * 32);
   if (e != cudaSuccess) {
-    wt_render_destroy(r);
+    release_renderer_buffers(r);
+    delete r;
     return fail(c, e == cudaErrorMemoryAllocation ? WT_ERR_NOMEM : WT_ERR_CUDA,
                 std::string("wt_render_create: ") + cudaGetErrorString(e));
   }
+  c->renderers.push_back(r);
   *out = r;
   return WT_OK;
 }

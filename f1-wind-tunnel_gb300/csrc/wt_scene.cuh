@@ -300,9 +300,9 @@ __device__ V2 sd_f1(const Scene& S, V3 pw) {
   const float lip = BODY_LIP * BODY_X;
   res.x = res.x * lip;
   if (sd_box(p - v3(0.24f, yw + 0.17f, 0.48f), v3(0.36f, 0.34f, 0.50f)) < dv(res.x, lip))
-    res = op_u(res, v2(sd_front_wing(S, p, yw) * lip, 7.0f));
+    res = op_u(res, v2(sd_front_wing(S, p, yw) * BODY_LIP * BODY_X, 7.0f));  // (d * LIP) * X, as written
   if (sd_box(p - v3(5.20f, b + 0.64f, 0.27f), v3(0.46f, 0.56f, 0.29f)) < dv(res.x, lip))
-    res = op_u(res, v2(sd_rear_wing(S, p, b, yr) * lip, 8.0f));
+    res = op_u(res, v2(sd_rear_wing(S, p, b, yr) * BODY_LIP * BODY_X, 8.0f));
   res = wheel_set(pworld, res, v3(FA, WR26, FWZ * BODY_Z), FHW26, 0.10f);
   res = wheel_set(pworld, res, v3(RA26, WR26, RWZ * BODY_Z), RHW26, 0.08f);
   return res;

@@ -49,6 +49,17 @@ void wto_voxelize(void* h, const void* shape) {
   memcpy(&s, shape, sizeof(s));
   with(h, [&](auto& L) { L.voxelize(s); });
 }
+// The scene SDF at n points (xyz): out[2k] distance, out[2k+1] material.
+void wto_scene_sdf(const void* shape, const float* pts, uint32_t n, float* out) {
+  wto::Shape s;
+  memcpy(&s, shape, sizeof(s));
+  wto::Sdf sdf(s);
+  for (uint32_t k = 0; k < n; k++) {
+    const wto::F2 r = sdf.scene(wto::f3(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]));
+    out[2 * k] = r.x;
+    out[2 * k + 1] = r.y;
+  }
+}
 void wto_set_solid(void* h, const uint32_t* solid, const float* emit) {
   with(h, [&](auto& L) {
     memcpy(L.solid.data(), solid, L.n * 4);

@@ -78,6 +78,7 @@ def _load_ref():
     L.wtr_blur.argtypes = [_vp, _i, _i, _vp, _i, _i, _vp]
     L.wtr_present.argtypes = [_vp, _i, _i, _vp, _i, _i, _vp, _i, _i, _vp, _vp]
     L.wtr_glow.argtypes = [_vp, _i, _i, _vp, _vp, ctypes.c_uint32, _vp, _vp, ctypes.c_uint32, _vp]
+    L.wtr_scene_sdf.argtypes = [_vp, _vp, ctypes.c_uint32, _vp]
     return L
 
 
@@ -166,6 +167,16 @@ def ref_render_scene(dims, origin, h, fields, temps, shape, cam, look, view, wid
     out = np.zeros((height, width, 4), np.float32)
     L.wtr_render_scene(d.ctypes.data, o.ctypes.data, ctypes.c_float(hh), f.ctypes.data, t.ctypes.data, w.ctypes.data,
                        _addr(cam), _addr(look), _addr(view), width, height, out.ctypes.data)
+    return out
+
+
+def ref_scene_sdf(shape, pts):
+    """The reference's sceneSdf at points [n, 3]: [n, 2] (distance, material)."""
+    L = ref_lib()
+    w = shape_words(shape)[:24].copy()
+    p = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    out = np.zeros((p.shape[0], 2), np.float32)
+    L.wtr_scene_sdf(w.ctypes.data, p.ctypes.data, p.shape[0], out.ctypes.data)
     return out
 
 

@@ -357,6 +357,18 @@ void wtr_render_scene(const uint32_t* dims, const float* origin, float h, const 
   });
 }
 
+// sceneSdf (the RENDER module's copy of the SDF chunk) at n points: out[2k], out[2k+1].
+void wtr_scene_sdf(const uint32_t* shape, const float* pts, uint32_t n, float* out) {
+  namespace M = m_render;
+  set_shape(M::shape, shape);
+  set_rig(M::rig);
+  for (uint32_t k = 0; k < n; k++) {
+    const rt::vec2f r = M::sceneSdf(rt::vec3f(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]));
+    out[2 * k] = r.x;
+    out[2 * k + 1] = r.y;
+  }
+}
+
 // TAA fs_main (render-wgsl.ts:456-518): cur and hist are w x h rgba16float targets;
 // taa: the Taa uniform (32 floats: prevViewProj column-major, camPos, tanHalf,
 // fwd, aspect, right, blend, up, pad).

@@ -396,9 +396,9 @@ struct Sdf {
     const float lip = BODY_LIP * BODY_X;
     res.x = res.x * lip;
     if (box(sub(p, f3(0.24f, yw + 0.17f, 0.48f)), f3(0.36f, 0.34f, 0.50f)) < res.x / lip)
-      res = op_u(res, f2(front_wing(p, yw) * lip, 7.0f));
+      res = op_u(res, f2(front_wing(p, yw) * BODY_LIP * BODY_X, 7.0f));  // (d * LIP) * X (f1.ts:309)
     if (box(sub(p, f3(5.20f, b + 0.64f, 0.27f)), f3(0.46f, 0.56f, 0.29f)) < res.x / lip)
-      res = op_u(res, f2(rear_wing(p, b, yr) * lip, 8.0f));
+      res = op_u(res, f2(rear_wing(p, b, yr) * BODY_LIP * BODY_X, 8.0f));
     res = wheel_set(pworld, res, f3(FA, WR26, FWZ * BODY_Z), FHW26, 0.10f);
     res = wheel_set(pworld, res, f3(RA26, WR26, RWZ * BODY_Z), RHW26, 0.08f);
     return res;

@@ -1,0 +1,90 @@
+// TEST INFRASTRUCTURE ONLY: the renderer's per-pixel device code
+// (f1-wind-tunnel_gb300/csrc/wt_shade.cuh: render_pixel, with the scene SDF,
+// field sampling and the project's math functions it calls) compiled for the
+// host, so that a CPU test can compare it with the reference's RENDER shader
+// translated to C++ at every pixel and at arbitrary SDF points.  CUDA
+// qualifiers become plain C++ and the device intrinsics their IEEE host
+// equivalents (correctly rounded division and square root, truncating float ->
+// unsigned).  Built with -ffp-contract=off like the product.
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <cuda_runtime.h>
+
+static inline float __fsqrt_rn(float x) { return sqrtf(x); }
+static inline float __fdiv_rn(float a, float b) { return a / b; }
+static inline unsigned int __float2uint_rz(float x) {
+  if (!(x > 0.0f)) return 0u;
+  if (x >= 4294967296.0f) return 4294967295u;
+  return (unsigned int)x;
+}
+template <class T>
+static inline T __ldg(const T* p) { return *p; }
+
+#include "wt_shade.cuh"
+
+using namespace wt;
+
+extern "C" {
+
+// RENDER fs_main over a w x h target: out[(y*w + x)*4 + k] = colour, hit distance.
+// shape: wt_shape; cam/look/view: the wt_cam / wt_look / wt_view structs;
+// fields (n x 4) and temps (n) of a lattice dims[3] at origin[3], spacing h.
+void wthm_render(const void* shape, const void* cam_p, const void* look_p, const void* view_p, const uint32_t* dims,
+                 const float* origin, float h, const float* fields, const float* temps, uint32_t w, uint32_t hgt,
+                 float* out) {
+  wt_cam cam;
+  wt_look look;
+  wt_view view;
+  memcpy(&cam, cam_p, sizeof cam);
+  memcpy(&look, look_p, sizeof look);
+  memcpy(&view, view_p, sizeof view);
+  SceneArgs a{};
+  memcpy(&a.shape, shape, sizeof a.shape);
+  a.g.nx = dims[0]; a.g.ny = dims[1]; a.g.nz = dims[2];
+  a.g.ox = origin[0]; a.g.oy = origin[1]; a.g.oz = origin[2]; a.g.h = h;
+  a.g.fields = reinterpret_cast<const float4*>(fields);
+  a.g.temps = temps;
+  a.view.uIn = view.u_in; a.view.vReal = view.v_real; a.view.cpMin = view.cp_min; a.view.cpMax = view.cp_max;
+  a.view.tMin = view.t_min; a.view.tMax = view.t_max; a.view.speedMax = view.speed_max; a.view.vortMax = view.vort_max;
+  auto f3 = [](const float* v) { return F3{v[0], v[1], v[2]}; };
+  auto f3n = [](float x, float y, float z) {
+    const float l = sqrtf(x * x + y * y + z * z);
+    return F3{x / l, y / l, z / l};
+  };
+  a.pos = f3(cam.pos); a.fwd = f3(cam.fwd); a.right = f3(cam.right); a.up = f3(cam.up);
+  a.tan_half = cam.tan_half; a.aspect = cam.aspect; a.time = cam.time; a.road_speed = cam.road_speed;
+  a.jitter_x = cam.jitter[0]; a.jitter_y = cam.jitter[1];
+  a.bmin = f3(look.bmin); a.bmax = f3(look.bmax);
+  a.paint_lin = F3{wtm::powf(look.paint[0], 2.2f), wtm::powf(look.paint[1], 2.2f), wtm::powf(look.paint[2], 2.2f)};
+  a.accent_lin = F3{wtm::powf(look.accent[0], 2.2f), wtm::powf(look.accent[1], 2.2f), wtm::powf(look.accent[2], 2.2f)};
+  a.surf_mode = look.surf_mode; a.palette = look.palette; a.carbon_body = look.carbon_body; a.is_f1 = look.is_f1;
+  a.slice_axis = look.slice_axis; a.show_flow = look.show_flow; a.slice_pos = look.slice_pos;
+  a.slice_alpha = look.slice_alpha;
+  a.key = f3n(-0.32f, 0.90f, 0.30f);
+  a.fill_a = f3n(0.6f, 0.35f, -0.7f);
+  a.fill_b = f3n(0.6f, 0.35f, 0.7f);
+  a.w = w; a.h = hgt;
+  const Scene S = make_scene(a.shape);
+  for (uint32_t y = 0; y < hgt; y++)
+    for (uint32_t x = 0; x < w; x++) {
+      const float4 c = render_pixel(S, a, x, y);
+      float* o = out + ((size_t)y * w + x) * 4;
+      o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
+    }
+}
+
+// sceneSdf at n points (xyz): out[2k] distance, out[2k+1] material.
+void wthm_scene_sdf(const void* shape, const float* pts, uint32_t n, float* out) {
+  wt_shape sh;
+  memcpy(&sh, shape, sizeof sh);
+  const Scene S = make_scene(sh);
+  for (uint32_t k = 0; k < n; k++) {
+    const V2 r = scene_sdf(S, v3(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]));
+    out[2 * k] = r.x;
+    out[2 * k + 1] = r.y;
+  }
+}
+
+}  // extern "C"

@@ -38,19 +38,26 @@ def test_render_frames_bitexact(setup):
     view = mc.view()
     for name, frames in seqs:
         r = R.Renderer(e, mr.W, mr.H)
-        for k, f in enumerate(frames):
-            u = r.frame(f["cam"], f["look"], view, parts=f.get("parts"), color_mode=f.get("color_mode", 0),
-                        smoke=f.get("smoke", True), lines=f.get("lines"), flow_time=f.get("flow_time", 0.0),
-                        vortices=f.get("vortices", False))
-            key = f"{name}_{k}"
-            got = {"scene": r.read(R.TARGET_SCENE), "hist": r.read(R.TARGET_HIST0 + u.cur),
-                   "glow": r.read(R.TARGET_GLOW), "bloom": r.read(R.TARGET_BLOOM_B)}
-            for t, v in got.items():
-                ref = z[f"{key}_{t}"]
-                bad = np.argwhere(np.any(v.view(np.uint16) != ref.view(np.uint16), axis=-1))
-                assert len(bad) == 0, f"{key} {t}: {len(bad)} texels differ, first {bad[:4].tolist()}"
-            assert np.array_equal(r.read(R.TARGET_OUTPUT), z[key + "_out"]), key
-        r.close()
+        try:
+            check_sequence(r, name, frames, z, view)
+        finally:
+            r.close()
+
+
+def check_sequence(r, name, frames, z, view):
+    from windtunnel import render as R
+    for k, f in enumerate(frames):
+        u = r.frame(f["cam"], f["look"], view, parts=f.get("parts"), color_mode=f.get("color_mode", 0),
+                    smoke=f.get("smoke", True), lines=f.get("lines"), flow_time=f.get("flow_time", 0.0),
+                    vortices=f.get("vortices", False))
+        key = f"{name}_{k}"
+        got = {"scene": r.read(R.TARGET_SCENE), "hist": r.read(R.TARGET_HIST0 + u.cur),
+               "glow": r.read(R.TARGET_GLOW), "bloom": r.read(R.TARGET_BLOOM_B)}
+        for t, v in got.items():
+            ref = z[f"{key}_{t}"]
+            bad = np.argwhere(np.any(v.view(np.uint16) != ref.view(np.uint16), axis=-1))
+            assert len(bad) == 0, f"{key} {t}: {len(bad)} texels differ, first {bad[:4].tolist()}"
+        assert np.array_equal(r.read(R.TARGET_OUTPUT), z[key + "_out"]), key
 
 
 def test_render_full_size_deterministic(setup):
@@ -89,3 +96,20 @@ def test_render_errors(setup):
         e._check(e.lib.wt_render_read(r.r, 9, np.zeros(4).ctypes.data), "wt_render_read")
     r.scene(u.cam, lk, mc.view())  # the renderer stays usable
     r.close()
+
+
+def test_renderer_outlives_its_context(wt_lib):
+    """Destroying the context first releases the renderer's targets; the handle
+    then only reports errors and can still be destroyed."""
+    from windtunnel import AeroEngine, WindTunnelError
+    from windtunnel import render as R
+    e = AeroEngine(dims=(16, 8, 8), h=0.2)
+    r = R.Renderer(e, 8, 4)
+    e.close()
+    rc = e.lib.wt_render_bloom(r.r)
+    assert rc != 0
+    r.close()
+    e2 = AeroEngine(dims=(16, 8, 8), h=0.2)
+    with pytest.raises(WindTunnelError, match="width and height"):
+        R.Renderer(e2, 0, 4)
+    e2.close()
