@@ -37,7 +37,7 @@ sys.path.insert(0, HERE)
 
 import make_consumers as mc  # noqa: E402
 from windtunnel import render as R  # noqa: E402
-from windtunnel.engine import ShapeKind  # noqa: E402
+from windtunnel.engine import ShapeKind, ShapeParams  # noqa: E402
 from windtunnel.workloads import config_f1_shape  # noqa: E402
 
 OUT = os.path.join(HERE, "render.npz")
@@ -45,18 +45,10 @@ W, H = 128, 72
 SHAPE_SEED = 3  # the consumer fixture's car
 
 
-class _Params:
-    """The shape fields make_look reads."""
-    kind = ShapeKind.F1
-
-    def __init__(self, shape):
-        self.ride_h = shape.ride_h
-
-
 def sequences(z):
     """[(name, [frame dict, ...]), ...]; each frame: camera, look, glow inputs."""
     shape = config_f1_shape(SHAPE_SEED)
-    p = _Params(shape)
+    p = ShapeParams(kind=ShapeKind.F1, rideH=shape.ride_h)  # the fields make_look reads
     parts = z["particles"][-1]
     asp = W / H
     hero = dict(cam=R.orbit_camera((2.75, 0.42, 0.0), 2.3, 0.3, 7.6, asp), look=R.make_look(p, palette=0),

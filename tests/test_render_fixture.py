@@ -88,3 +88,58 @@ def test_orbit_camera_and_jitter():
     b = st.next(cam, (128, 72))
     assert (a.cur, b.cur) == (1, 0) and a.taa.blend == 1.0 and abs(b.taa.blend - 0.1) < 1e-7
     assert abs(a.cam.jitter[0] - (R.halton(2, 2) - 0.5) * 2 / 128) < 1e-7
+
+
+def _viewer_without_gpu(shape_params, kmh=250.0, flow_mode=None):
+    """A Viewer's host-side state over a stand-in engine (no device calls)."""
+    from types import SimpleNamespace
+    from windtunnel.viewer import FlowMode, Viewer, ViewParams
+    v = object.__new__(Viewer)
+    v.engine = SimpleNamespace(shape_params=shape_params, h=10.4 / 232, u_lb=0.0925, dims=(232, 68, 52))
+    v.view = ViewParams(kmh=kmh, flow_mode=FlowMode.Streamlines if flow_mode is None else flow_mode)
+    v.flow_time = 0.25
+    return v
+
+
+def test_viewer_uniforms_follow_the_engine():
+    from windtunnel.engine import ORIGIN_X, ShapeKind, ShapeParams
+    from windtunnel.viewer import MAX_LINES, STREAM_STEPS, FlowMode
+    f1 = ShapeParams(kind=ShapeKind.F1, rideH=0.10)
+    v = _viewer_without_gpu(f1)
+    s = v.stream_params()                                    # streamConfig (engine.ts:558-570)
+    assert (s.lines, s.rows, s.cols, s.seed_mode, s.steps) == (90, 18, 5, 0, STREAM_STEPS)
+    assert list(s.seed_min) == pytest.approx([-1.2, 0.05, 0.03]) and list(s.seed_max) == pytest.approx([0, 1.3, 0.95])
+    assert abs(s.step_len - 0.03) < 1e-7 and abs(s.time - 0.25) < 1e-7
+    vx = _viewer_without_gpu(f1, flow_mode=FlowMode.Vortices).stream_params()
+    assert (vx.seed_mode, vx.emitters, vx.per_emitter, vx.lines) == (1, 4, MAX_LINES // 4, MAX_LINES // 4 * 4)
+    yw, yr = 0.19 + 0.10 * 0.45, 0.10 + 0.8
+    assert list(vx.emitter[0]) == pytest.approx([0.52, yw + 0.2, 0.926, 0.06])
+    assert list(vx.emitter[2]) == pytest.approx([5.36, yr + 0.26, 0.494, 0.06])
+    lo, hi, rows, cols = v.spawn_region()                    # spawnRegion (engine.ts:731-737)
+    assert lo == pytest.approx((ORIGIN_X + 2 * 10.4 / 232, 0.04, 0.0)) and (rows, cols) == (12, 7)
+    assert hi == pytest.approx((0.0, 0.10 + 1.34 + 0.25, 0.98 + 0.25))
+    u = v.view_uniform()                                     # viewUniform (engine.ts:503-518)
+    assert (u.t_min, u.t_max, u.cp_min) == pytest.approx((0.0, 220.0, -1.1))
+    cold = _viewer_without_gpu(ShapeParams(kind=ShapeKind.F1, heatBrakes=False, heatEngine=False, heatRad=False))
+    stag = 0.5 * (250 / 3.6) ** 2 / 1005
+    assert (cold.view_uniform().t_min, cold.view_uniform().t_max) == pytest.approx((-stag * 1.4, stag * 1.05))
+    assert _viewer_without_gpu(f1, kmh=500).visual_flow_rate() == 1.6
+    assert _viewer_without_gpu(f1, kmh=50).visual_flow_rate() == 0.35
+
+
+def test_write_png_roundtrip(tmp_path):
+    import struct
+    import zlib
+    from windtunnel.viewer import write_png
+    img = (np.arange(5 * 7 * 4) % 251).astype(np.uint8).reshape(5, 7, 4)
+    p = tmp_path / "a.png"
+    write_png(str(p), img)
+    b = p.read_bytes()
+    assert b[:8] == b"\x89PNG\r\n\x1a\n"
+    w, h = struct.unpack(">II", b[16:24])
+    assert (w, h) == (7, 5)
+    i = b.index(b"IDAT")
+    n = struct.unpack(">I", b[i - 4:i])[0]
+    raw = zlib.decompress(b[i + 4:i + 4 + n])
+    rows = [raw[r * (7 * 4 + 1) + 1:(r + 1) * (7 * 4 + 1)] for r in range(5)]
+    assert np.array_equal(np.frombuffer(b"".join(rows), np.uint8).reshape(5, 7, 4), img)
