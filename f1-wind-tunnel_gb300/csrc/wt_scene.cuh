@@ -104,7 +104,9 @@ __device__ float sd_cyl_z(V3 p, float r, float hz) {
   const float dx = len2(v2(p.x, p.y)) - r, dz = ab(p.z) - hz;
   return mn(mx(dx, dz), 0.0f) + len2(v2(mx(dx, 0.0f), mx(dz, 0.0f)));
 }
-__device__ float sd_wing_z(V3 p, V2 le, float chord, float ang, float thick, float z0, float z1, float rise,
+// Out of line (as is wheel_set): sixteen call sites would otherwise each carry a
+// copy, with its sin/cos, and the SDF's code would outgrow the instruction cache.
+__device__ __noinline__ float sd_wing_z(V3 p, V2 le, float chord, float ang, float thick, float z0, float z1, float rise,
                            float taper, float curl) {
   const float s = sstep(curl, z1, p.z);
   return sd_wing(p, le + v2(0.0f, rise * s), chord * (1.0f - taper * s), ang + rise * s * 0.6f, thick, z0, z1) *
@@ -147,7 +149,7 @@ __device__ float sd_wheel_cover(V3 p, V3 c, float hw) {
   d = mn(d, sd_cyl_z(q - v3(0.0f, 0.0f, hw - 0.02f), 0.045f, 0.02f));
   return d;
 }
-__device__ V2 wheel_set(V3 p, V2 res, V3 c, float hw, float inboard) {
+__device__ __noinline__ V2 wheel_set(V3 p, V2 res, V3 c, float hw, float inboard) {
   if (sd_box(p - c, v3(WR26 + 0.02f, WR26 + 0.02f, hw + 0.2f)) > res.x) return res;
   res = op_u(res, v2(sd_tyre(p, c, hw), 2.0f));
   res = op_u(res, v2(sd_wheel_cover(p, c, hw), 9.0f));

@@ -131,18 +131,19 @@ __device__ V2 box_hit(V3 ro, V3 rd, V3 bmin, V3 bmax) {
   return v2(mx(mx(tn.x, tn.y), tn.z), mn(mn(tf.x, tf.y), tf.z));
 }
 
-struct Ctx {
-  const Scene& S;
-  const SceneArgs& a;
-};
+// One out-of-line copy of the scene SDF for the whole pass: the ray march,
+// normal, occlusion, shadow and reflection taps all call it, and inlining it
+// at each site multiplies the code past the instruction cache.
+__device__ __noinline__ V2 sdf(const Scene& S, V3 p) { return scene_sdf(S, p); }
+
 
 // march (render-wgsl.ts:68-79)
-__device__ V2 march(const Ctx& c, V3 ro, V3 rd, int max_steps) {
-  const V2 tb = box_hit(ro, rd, c3(c.a.bmin), c3(c.a.bmax));
+__device__ __noinline__ V2 march(const Scene& S, const SceneArgs& a, V3 ro, V3 rd, int max_steps) {
+  const V2 tb = box_hit(ro, rd, c3(a.bmin), c3(a.bmax));
   if (tb.x > tb.y || tb.y < 0.0f) return v2(FAR, 0.0f);
   float t = mx(tb.x, 0.0f);
   for (int i = 0; i < max_steps; i++) {
-    const V2 r = scene_sdf(c.S, ro + rd * t);
+    const V2 r = sdf(S, ro + rd * t);
     if (r.x < 0.0004f * t + 0.0003f) return v2(t, r.y);
     t = t + r.x * 0.9f;
     if (t > tb.y) break;
@@ -150,31 +151,31 @@ __device__ V2 march(const Ctx& c, V3 ro, V3 rd, int max_steps) {
   return v2(FAR, 0.0f);
 }
 // calcNormal (render-wgsl.ts:80-83): e = (1, -1) * 0.0008
-__device__ V3 calc_normal(const Ctx& c, V3 p) {
+__device__ V3 calc_normal(const Scene& S, const SceneArgs& a, V3 p) {
   const float ex = 0.0008f, ey = -0.0008f;
   const V3 xyy = v3(ex, ey, ey), yyx = v3(ey, ey, ex), yxy = v3(ey, ex, ey), xxx = v3(ex, ex, ex);
-  const V3 s = xyy * scene_sdf(c.S, p + xyy).x + yyx * scene_sdf(c.S, p + yyx).x + yxy * scene_sdf(c.S, p + yxy).x +
-               xxx * scene_sdf(c.S, p + xxx).x;
+  const V3 s = xyy * sdf(S, p + xyy).x + yyx * sdf(S, p + yyx).x + yxy * sdf(S, p + yxy).x +
+               xxx * sdf(S, p + xxx).x;
   return nrm3(s);
 }
 // ambientOcc (render-wgsl.ts:84-93)
-__device__ float ambient_occ(const Ctx& c, V3 p, V3 n) {
+__device__ float ambient_occ(const Scene& S, const SceneArgs& a, V3 p, V3 n) {
   float occ = 0.0f, sca = 1.0f;
   for (int i = 1; i <= 5; i++) {
     const float hh = 0.012f + 0.03f * (float)i;
-    occ = occ + (hh - scene_sdf(c.S, p + n * hh).x) * sca;
+    occ = occ + (hh - sdf(S, p + n * hh).x) * sca;
     sca = sca * 0.75f;
   }
   return clmp(1.0f - 2.2f * occ, 0.0f, 1.0f);
 }
 // softShadow (render-wgsl.ts:94-107)
-__device__ float soft_shadow(const Ctx& c, V3 ro, V3 rd) {
-  const V2 tb = box_hit(ro, rd, c3(c.a.bmin), c3(c.a.bmax));
+__device__ float soft_shadow(const Scene& S, const SceneArgs& a, V3 ro, V3 rd) {
+  const V2 tb = box_hit(ro, rd, c3(a.bmin), c3(a.bmax));
   if (tb.x > tb.y || tb.y < 0.0f) return 1.0f;
   float t = mx(tb.x, 0.01f);
   float res = 1.0f;
   for (int i = 0; i < 48; i++) {
-    const float hh = scene_sdf(c.S, ro + rd * t).x;
+    const float hh = sdf(S, ro + rd * t).x;
     res = mn(res, 12.0f * hh / t);
     if (res < 0.01f || t > tb.y) break;
     t = t + clmp(hh, 0.01f, 0.2f);
@@ -248,9 +249,7 @@ __device__ Mat livery_body(const Scene& S, V3 p, float b, V3 silver, V3 teal) {
 }
 
 // materialAt (render-wgsl.ts:180-255) for the analytic scenes (look.meshMode == 0).
-__device__ Mat material_at(const Ctx& c, float m, V3 pw, V3 n, float vd) {
-  const Scene& S = c.S;
-  const SceneArgs& a = c.a;
+__device__ __noinline__ Mat material_at(const Scene& S, const SceneArgs& a, float m, V3 pw, V3 n, float vd) {
   const V3 pabs = v3(pw.x, pw.y, ab(pw.z));
   const V3 p = a.is_f1 != 0u ? body_frame(S, pabs) : pabs;
   const float b = S.s.ride_h;
@@ -326,16 +325,16 @@ __device__ Mat material_at(const Ctx& c, float m, V3 pw, V3 n, float vd) {
 }
 
 // shadeSurface (render-wgsl.ts:257-283); lift = 0.004 without the baked mesh
-__device__ V3 shade_surface(const Ctx& c, V3 p, V3 n, V3 rd, const Mat& mt, bool fast) {
-  const V3 key = c3(c.a.key);
+__device__ __noinline__ V3 shade_surface(const Scene& S, const SceneArgs& a, V3 p, V3 n, V3 rd, const Mat mt, bool fast) {
+  const V3 key = c3(a.key);
   float sh = 1.0f, ao = 1.0f;
   const float lift = 0.004f;
   if (!fast) {
-    sh = soft_shadow(c, p + n * lift, key);
-    ao = ambient_occ(c, p + n * (lift - 0.004f), n);
+    sh = soft_shadow(S, a, p + n * lift, key);
+    ao = ambient_occ(S, a, p + n * (lift - 0.004f), n);
   }
   const float ndl = mx(dot3(n, key), 0.0f);
-  const float fill = mx(dot3(n, c3(c.a.fill_a)), 0.0f) * 0.18f + mx(dot3(n, c3(c.a.fill_b)), 0.0f) * 0.18f;
+  const float fill = mx(dot3(n, c3(a.fill_a)), 0.0f) * 0.18f + mx(dot3(n, c3(a.fill_b)), 0.0f) * 0.18f;
   const float amb = (0.45f + 0.55f * n.y) * 0.22f * ao;
   const V3 h = nrm3(key - rd);
   const float rough = mt.rough;
@@ -358,7 +357,6 @@ __device__ V3 shade_surface(const Ctx& c, V3 p, V3 n, V3 rd, const Mat& mt, bool
 
 // RENDER fs_main (render-wgsl.ts:288-398) for pixel (x, y): colour and hit distance.
 __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, uint32_t y) {
-  const Ctx c{S, a};
   const float ux = ((float)x + 0.5f) / (float)a.w, uy = ((float)y + 0.5f) / (float)a.h;
   const float ndx = (ux * 2.0f - 1.0f) + a.jitter_x, ndy = (1.0f - uy * 2.0f) + a.jitter_y;
   const V3 rd = nrm3(c3(a.fwd) + ndx * a.tan_half * a.aspect * c3(a.right) + ndy * a.tan_half * c3(a.up));
@@ -367,15 +365,15 @@ __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, u
 
   V3 col = backdrop(rd);
   float t_hit = FAR;
-  const V2 hit = march(c, ro, rd, 220);
+  const V2 hit = march(S, a, ro, rd, 220);
   float t_ground = FAR;
   if (rd.y < -1e-4f) t_ground = -ro.y / rd.y;
 
   if (hit.x < t_ground && hit.x < FAR) {
     const V3 p = ro + rd * hit.x;
     const float vd = hit.x;
-    const V3 n = calc_normal(c, p);
-    Mat mt = material_at(c, hit.y, p, n, vd);
+    const V3 n = calc_normal(S, a, p);
+    Mat mt = material_at(S, a, hit.y, p, n, vd);
     if (a.surf_mode == 1u) {
       V3 probe = p + n * a.g.h * 0.8f;
       Sample s = sample_flow(a.g, probe);
@@ -389,7 +387,7 @@ __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, u
         mt = mat(tolinear(palette(a.palette, v)) * iso, 0.55f, 0.0f, 0.25f, zero3());
       }
     }
-    col = shade_surface(c, p, n, rd, mt, false);
+    col = shade_surface(S, a, p, n, rd, mt, false);
     t_hit = hit.x;
   } else if (t_ground < FAR) {
     const V3 p = ro + rd * t_ground;
@@ -402,18 +400,18 @@ __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, u
       gc = gc * 0.75f + v3(0.006f, 0.006f, 0.006f) * sstep(0.0f, 0.08f, stripe) * sstep(0.2f, 0.12f, stripe);
       gc = gc + v3(0.05f, 0.05f, 0.055f) * (1.0f - sstep(0.0f, 0.012f, ab(ab(p.z) - 1.15f))) * pool;
     }
-    const float sh = soft_shadow(c, p + up * 0.005f, key);
-    const float ao = clmp(scene_sdf(S, p).x * 2.6f + 0.12f, 0.0f, 1.0f);
+    const float sh = soft_shadow(S, a, p + up * 0.005f, key);
+    const float ao = clmp(sdf(S, p).x * 2.6f + 0.12f, 0.0f, 1.0f);
     col = gc * (0.35f + 0.65f * sh) * mixf(0.25f, 1.0f, ao);
     const V3 rdir = reflect3(rd, up);
     const float fres = 0.02f + 0.22f * wtm::powf(1.0f - ab(rd.y), 5.0f);
     V3 refl = studio_env(rdir) * 0.35f;
-    const V2 rh = march(c, p + up * 0.002f, rdir, 90);
+    const V2 rh = march(S, a, p + up * 0.002f, rdir, 90);
     if (rh.x < FAR) {
       const V3 rp = p + rdir * rh.x;
-      const V3 rn = calc_normal(c, rp);
+      const V3 rn = calc_normal(S, a, rp);
       const float vd = t_ground + rh.x;
-      refl = shade_surface(c, rp, rn, rdir, material_at(c, rh.y, rp, rn, vd), true) * wtm::expf(-rh.x * 2.2f);
+      refl = shade_surface(S, a, rp, rn, rdir, material_at(S, a, rh.y, rp, rn, vd), true) * wtm::expf(-rh.x * 2.2f);
     }
     col = col + refl * fres * ao;
     const float fog_t = 1.0f - wtm::expf(-t_ground * 0.03f);

@@ -21,6 +21,12 @@ static inline unsigned int __float2uint_rz(float x) {
 }
 template <class T>
 static inline T __ldg(const T* p) { return *p; }
+// system headers first: libstdc++ spells its own attributes with __noinline__
+#include "wt_fields.h"
+#include "wt_internal.h"
+#ifndef __noinline__
+#define __noinline__ __attribute__((__noinline__))
+#endif
 
 #include "wt_shade.cuh"
 
