@@ -281,13 +281,113 @@ def run_surrogate(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_render(args, rank, world):
+    """The render passes of the headless check's hero frame at 1280x720 (scene
+    ray march, TAA, streamline glow, bloom, present) over a developed flow of
+    the generic F1 at the medium quality (232x68x52): ms per frame.  e2e: the
+    whole engine frame through the public API (8 LBM steps, heat, the
+    streamline pass, the render passes) with the RGBA8 image read back."""
+    import numpy as np
+    import torch
+    from oracle import pyoracle
+    from windtunnel import AeroEngine
+    from windtunnel.render import FrameState, make_look
+    from windtunnel.viewer import HEADLESS_SHAPE, Viewer, orbit
+    W, H = 1280, 720
+    eng = AeroEngine("medium")
+    viewer = Viewer(eng, W, H, particles=1)
+    eng.set_shape(HEADLESS_SHAPE)
+    eng.reset()
+    cam = orbit({}, W / H)
+    for _ in range(40):                       # develop the flow
+        viewer.frame(cam, 8)
+    view = viewer.view_uniform()
+    sp = viewer.stream_params()
+    lines = eng.streamlines(sp, view)
+    look = make_look(HEADLESS_SHAPE)
+    r = viewer.renderer
+    stream = torch.cuda.ExternalStream(eng.stream())
+
+    def passes():
+        r.frame(cam, look, view, lines=lines, flow_time=0.5)
+
+    for _ in range(max(3, args.warmup)):
+        passes()
+    eng.sync()
+    steps = max(5, min(args.steps, 60))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            passes()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # the scene pass alone (the dominant kernel)
+    u = FrameState().next(cam, (W, H), lines=lines)
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(steps):
+        r.scene(u.cam, look, view)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    scene_ms = s0.elapsed_time(s1) / steps
+    # end to end: whole frames through the public API, image read back each frame
+    e2e_frames = max(5, min(args.steps, 30))
+    t0 = time.perf_counter()
+    for _ in range(e2e_frames):
+        viewer.frame(cam, 8)
+        img = viewer.image()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_frames
+    line_bytes = sp.lines * sp.steps * 16
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the render passes' dominant part, the scene pass, in the device code built
+        # for the host, on all host cores: a band of rows, scaled to the full frame
+        from windtunnel.engine import pack_shape
+        if pyoracle.shade_model_lib() is not None:
+            cores = os.cpu_count() or 1
+            d = eng.debug_read()
+            rows = list(range(0, H, 10))
+            t0 = time.perf_counter()
+            pyoracle.shade_model_render(pack_shape(HEADLESS_SHAPE), u.cam, look, view, eng.dims, eng.origin, eng.h,
+                                        d["fields"], d["temps"], W, H, threads=cores, rows=rows)
+            dt = time.perf_counter() - t0
+            base = {"value": dt * 1e3 * H / len(rows), "unit": "ms/frame", "cores": cores, "kind": "port",
+                    "sample": f"scene pass (RENDER fs_main) on every 10th row ({len(rows)} of {H}) of the 1280x720 "
+                              "frame, device shading code compiled for the host, one row per task over all cores, "
+                              "scaled by rows"}
+    if rank == 0:
+        clocks = clk.summary()
+        print(json.dumps({
+            "metric": "render_ms_per_frame", "value": ms, "unit": "ms", "n_gpus": world, "steps": steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "headless-check hero frame at 1280x720: scene ray march of the generic F1, TAA, "
+                                   "streamline glow (90 lines x 360 points), bloom, present; medium lattice "
+                                   "232x68x52 after 40 frames",
+                       "image": [W, H], "scene_pass_ms": scene_ms,
+                       "l2": "targets (29 MB) fit L2: the passes are compute-bound, no flush"},
+            "roofline": None,
+            "roofline_note": "scene pass: ALU / instruction-issue bound ray march, not HBM or tensor; "
+                             "issue utilisation in profiles/render_scene_f1_1280x720.md",
+            "cpu_baseline": base,
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": line_bytes + 4 * 24 * 4,
+                    "d2h_bytes_per_step": line_bytes + W * H * 4},
+            "gpu_launches": steps * 7,
+            "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+        }), flush=True)
+    viewer.close()
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200, help="timed frames")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="wt", choices=["wt", "reference"])
-    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "surrogate"])
+    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "surrogate", "render"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-frames", type=int, default=4)
@@ -328,6 +428,11 @@ def main():
     from windtunnel.workloads import bytes_per_lup
     if args.workload == "surrogate":
         run_surrogate(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload == "render":
+        run_render(args, rank, world)
         if dist:
             dist.destroy_process_group()
         return

@@ -82,6 +82,47 @@ def _load_ref():
     return L
 
 
+SHADE_SO = os.path.join(HERE, "_build", "libshadehm.so")
+_S = None
+
+
+def shade_model_lib():
+    """The renderer's device shading code built for the host (shade_host_model.cpp),
+    or None where it cannot be built (no CUDA headers)."""
+    global _S
+    if _S is None:
+        r = subprocess.run(["make", "-s", "-C", HERE, "_build/libshadehm.so"], capture_output=True, text=True)
+        if r.returncode != 0 or not os.path.exists(SHADE_SO):
+            return None
+        L = ctypes.CDLL(SHADE_SO)
+        L.wthm_render.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _F, _vp, _vp] + [ctypes.c_uint32] * 4 + [_vp]
+        L.wthm_scene_sdf.argtypes = [_vp, _vp, ctypes.c_uint32, _vp]
+        _S = L
+    return _S
+
+
+def shade_model_render(shape, cam, look, view, dims, origin, h, fields, temps, width, height, threads=1, rows=None):
+    """RENDER fs_main of the device code on the host: [height, width, 4] float32
+    (colour, hit distance) for the given rows (default all), one row per task
+    over `threads` host threads."""
+    import concurrent.futures as cf
+    L = shade_model_lib()
+    d = np.ascontiguousarray(dims, np.uint32)
+    o = np.ascontiguousarray(origin, np.float32)
+    f = np.ascontiguousarray(fields, np.float32)
+    t = np.ascontiguousarray(temps, np.float32)
+    out = np.zeros((height, width, 4), np.float32)
+
+    def run(y):
+        L.wthm_render(ctypes.addressof(shape), ctypes.addressof(cam), ctypes.addressof(look), ctypes.addressof(view),
+                      d.ctypes.data, o.ctypes.data, float(h), f.ctypes.data, t.ctypes.data, width, height,
+                      int(y), int(y) + 1, out.ctypes.data)
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        list(ex.map(run, range(height) if rows is None else rows))
+    return out
+
+
 _O = None
 _R = None
 

@@ -1,4 +1,5 @@
-// TEST INFRASTRUCTURE ONLY: the renderer's per-pixel device code
+// TEST INFRASTRUCTURE ONLY (the checker and the render workload's CPU
+// baseline, never the product): the renderer's per-pixel device code
 // (f1-wind-tunnel_gb300/csrc/wt_shade.cuh: render_pixel, with the scene SDF,
 // field sampling and the project's math functions it calls) compiled for the
 // host, so that a CPU test can compare it with the reference's RENDER shader
@@ -34,12 +35,13 @@ using namespace wt;
 
 extern "C" {
 
-// RENDER fs_main over a w x h target: out[(y*w + x)*4 + k] = colour, hit distance.
-// shape: wt_shape; cam/look/view: the wt_cam / wt_look / wt_view structs;
-// fields (n x 4) and temps (n) of a lattice dims[3] at origin[3], spacing h.
+// RENDER fs_main over rows [y0, y1) of a w x h target: out[(y*w + x)*4 + k] =
+// colour, hit distance (rows outside the range untouched).  shape: wt_shape;
+// cam/look/view: the wt_cam / wt_look / wt_view structs; fields (n x 4) and
+// temps (n) of a lattice dims[3] at origin[3], spacing h.
 void wthm_render(const void* shape, const void* cam_p, const void* look_p, const void* view_p, const uint32_t* dims,
                  const float* origin, float h, const float* fields, const float* temps, uint32_t w, uint32_t hgt,
-                 float* out) {
+                 uint32_t y0, uint32_t y1, float* out) {
   wt_cam cam;
   wt_look look;
   wt_view view;
@@ -73,7 +75,7 @@ void wthm_render(const void* shape, const void* cam_p, const void* look_p, const
   a.fill_b = f3n(0.6f, 0.35f, 0.7f);
   a.w = w; a.h = hgt;
   const Scene S = make_scene(a.shape);
-  for (uint32_t y = 0; y < hgt; y++)
+  for (uint32_t y = y0; y < y1 && y < hgt; y++)
     for (uint32_t x = 0; x < w; x++) {
       const float4 c = render_pixel(S, a, x, y);
       float* o = out + ((size_t)y * w + x) * 4;

@@ -59,34 +59,7 @@ def replay(sim_obj, man, case, read):
 
 def shade_host_model():
     """The renderer's per-pixel device code built for the host
-    (tests/cuda/shade_host_model.cpp) as a ctypes library, or None where g++ or
-    the CUDA headers are missing.  Cached in the temp directory by source hash."""
-    import ctypes
-    import shutil
-    import subprocess
-    import tempfile
-    src = os.path.join(ROOT, "tests", "cuda", "shade_host_model.cpp")
-    csrc = os.path.join(ROOT, "f1-wind-tunnel_gb300", "csrc")
-    cuda_inc = None
-    for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
-        if cand and os.path.exists(os.path.join(cand, "include", "cuda_runtime.h")):
-            cuda_inc = os.path.join(cand, "include")
-            break
-    gxx = shutil.which("g++")
-    if cuda_inc is None or gxx is None:
-        return None
-    h = hashlib.sha256()
-    for f in [src, os.path.join(ROOT, "include", "wt.h")] + sorted(
-            os.path.join(csrc, n) for n in os.listdir(csrc) if n.endswith((".cuh", ".h"))):
-        h.update(open(f, "rb").read())
-    so = os.path.join(tempfile.gettempdir(), f"wt_shade_host_model_{h.hexdigest()[:16]}.so")
-    if not os.path.exists(so):
-        tmp = so + f".{os.getpid()}.tmp"
-        subprocess.run([gxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-                        "-I", os.path.join(ROOT, "include"), "-I", csrc, "-I", cuda_inc, "-o", tmp, src], check=True)
-        os.replace(tmp, so)
-    L = ctypes.CDLL(so)
-    vp = ctypes.c_void_p
-    L.wthm_render.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_float, vp, vp, ctypes.c_uint32, ctypes.c_uint32, vp]
-    L.wthm_scene_sdf.argtypes = [vp, vp, ctypes.c_uint32, vp]
-    return L
+    (oracle/shade_host_model.cpp) as a ctypes library, or None where the CUDA
+    headers are missing."""
+    from oracle import pyoracle
+    return pyoracle.shade_model_lib()

@@ -1,6 +1,6 @@
 """The scene signed-distance field at arbitrary points, bit for bit, in its
 three implementations: the device code (wt_scene.cuh, built for the host by
-tests/cuda/shade_host_model.cpp), the oracle's restatement (oracle/wt_oracle.hpp)
+oracle/shade_host_model.cpp), the oracle's restatement (oracle/wt_oracle.hpp)
 and the reference's own SDF chunk translated to C++ (render module).  Rays and
 shadow probes sample the field everywhere (both sides of the symmetry plane,
 below the ground, inside bodies), not only at cell centres where the
@@ -23,7 +23,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 def hm():
     L = shade_host_model()
     if L is None:
-        pytest.skip("g++ or the CUDA headers are missing")
+        pytest.skip("the CUDA headers are missing")
     return L
 
 
@@ -81,10 +81,9 @@ def test_device_render_pixel_matches_fixture(hm):
         st = R.FrameState()
         for k, f in enumerate(frames):
             u = mr.frame_uniforms(st, f)
-            out = np.zeros((mr.H, mr.W, 4), np.float32)
-            hm.wthm_render(ctypes.addressof(shape), ctypes.addressof(u.cam), ctypes.addressof(f["look"]),
-                           ctypes.addressof(view), dims.ctypes.data, org.ctypes.data, mc.H, c["fields"].ctypes.data,
-                           c["temps"].ctypes.data, mr.W, mr.H, out.ctypes.data)
+            from oracle import pyoracle
+            out = pyoracle.shade_model_render(shape, u.cam, f["look"], view, dims, org, mc.H, c["fields"], c["temps"],
+                                              mr.W, mr.H, threads=4)
             ref = z[f"{name}_{k}_scene"]
             bad = np.argwhere(np.any(out.astype(np.float16).view(np.uint16) != ref.view(np.uint16), axis=-1))
             assert len(bad) == 0, f"{name}_{k}: {len(bad)} pixels differ, first {bad[:4].tolist()}"
