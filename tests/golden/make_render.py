@@ -10,13 +10,16 @@ after five passes and its streamlines).  The fixed-function stages (viewport,
 rasterization, blending) are the oracle's restatement of the WebGPU pipeline
 (oracle/ref_driver.cpp).
 
-Five sequences of frames at 128x72 cover the scene pass's branches:
+Nine sequences of frames at 128x72 cover the scene pass's branches:
   hero      livery, ground reflection and belt, streamline glow; then a second
             frame from a slightly moved camera, which reprojects the history
   surface   pressure colour on the body surface (surfMode 1, palette 1)
   slice-z   z slice with temperature colours, particle glow (palette 2)
   slice-x   x slice with vorticity colours, vortex streamlines (palette 3)
   slice-y   y slice with the wake map (palette 4), a carbon-free paint livery
+  cube, sphere, wing, empty
+            the other analytic scenes: carbon and paint bodies, vorticity colour
+            on a sphere's surface, a pressure slice past the wing, the bare tunnel
 Stored per frame: the scene, resolved history, glow and bloom B targets
 (binary16) and the presented RGBA8 output.
 
@@ -64,8 +67,32 @@ def sequences(z):
     slice_y = dict(cam=R.orbit_camera((2.5, 0.4, 0.0), 0.6, 0.5, 6.5, asp),
                    look=R.make_look(p, palette=4, slice_axis=2, slice_pos=0.3, paint=(0.7, 0.1, 0.1), carbon=False),
                    parts=parts, color_mode=4, smoke=False)
-    return shape, [("hero", [hero, hero2]), ("surface", [surface]), ("slice-z", [slice_z]), ("slice-x", [slice_x]),
-                   ("slice-y", [slice_y])]
+    seqs = [("hero", [hero, hero2]), ("surface", [surface]), ("slice-z", [slice_z]), ("slice-x", [slice_x]),
+            ("slice-y", [slice_y])]
+    # the other analytic scenes (engine.ts:474-486 bounds), over the same flow
+    cube = ShapeParams(kind=ShapeKind.Cube)
+    sphere = ShapeParams(kind=ShapeKind.Sphere)
+    wing = ShapeParams(kind=ShapeKind.Wing, aoaDeg=8.0)
+    empty = ShapeParams(kind=ShapeKind.Empty)
+    seqs += [
+        ("cube", [dict(cam=R.orbit_camera((2.6, 1.0, 0.0), 2.2, 0.35, 4.5, asp), look=R.make_look(cube, palette=0),
+                       parts=parts, color_mode=0, smoke=True, shape=cube)]),
+        ("sphere", [dict(cam=R.orbit_camera((2.6, 1.0, 0.0), 2.6, 0.25, 3.8, asp),
+                         look=R.make_look(sphere, palette=3, surface_field=True, carbon=False, paint=(0.2, 0.5, 0.9)),
+                         shape=sphere)]),
+        ("wing", [dict(cam=R.orbit_camera((2.4, 1.2, 0.0), 1.7, 0.3, 6.0, asp),
+                       look=R.make_look(wing, palette=1, slice_axis=3, slice_pos=0.2, carbon=False),
+                       lines=z["lines_rake"], color_mode=1, flow_time=0.2, shape=wing)]),
+        ("empty", [dict(cam=R.orbit_camera((2.0, 0.5, 0.0), 2.0, 0.4, 7.0, asp),
+                        look=R.make_look(empty, palette=0, slice_axis=2, slice_pos=0.5), shape=empty)]),
+    ]
+    return shape, seqs
+
+
+def frame_shape(default, f):
+    """The wt_shape a frame renders: its own analytic scene, or the fixture's F1."""
+    from windtunnel.engine import pack_shape
+    return pack_shape(f["shape"]) if "shape" in f else default
 
 
 def frame_uniforms(state, f):
@@ -86,8 +113,8 @@ def main():
         hist = [np.zeros((H, W, 4), np.float32), np.zeros((H, W, 4), np.float32)]
         for k, f in enumerate(frames):
             u = frame_uniforms(st, f)
-            scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, z["fields"], z["temps"], shape, u.cam, f["look"],
-                                              view, W, H)
+            scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, z["fields"], z["temps"], frame_shape(shape, f),
+                                              u.cam, f["look"], view, W, H)
             hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)
             glow = pyoracle.ref_glow(scene, f.get("parts"), u.pdraw, f.get("lines"), u.sdraw)
             ba = pyoracle.ref_blur(glow, (1.0, 0.0), 3.0, 1.0, hw, hh)

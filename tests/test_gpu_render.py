@@ -28,15 +28,17 @@ def setup(wt_lib):
     shape, seqs = mr.sequences(c)
     e.set_shape_raw(shape)
     e.write_state(fields=c["fields"], temps=c["temps"])
-    yield mc, mr, z, e, seqs
+    yield mc, mr, z, e, seqs, shape, c
     e.close()
 
 
 def test_render_frames_bitexact(setup):
     from windtunnel import render as R
-    mc, mr, z, e, seqs = setup
+    mc, mr, z, e, seqs, shape, c = setup
     view = mc.view()
     for name, frames in seqs:
+        e.set_shape_raw(mr.frame_shape(shape, frames[0]))  # the renderer draws the context's shape
+        e.write_state(fields=c["fields"], temps=c["temps"])
         r = R.Renderer(e, mr.W, mr.H)
         try:
             check_sequence(r, name, frames, z, view)
@@ -63,7 +65,9 @@ def check_sequence(r, name, frames, z, view):
 def test_render_full_size_deterministic(setup):
     """1280x720 (the headless check's size): finite targets, identical on a rerun."""
     from windtunnel import render as R
-    mc, mr, z, e, seqs = setup
+    mc, mr, z, e, seqs, shape, c = setup
+    e.set_shape_raw(shape)
+    e.write_state(fields=c["fields"], temps=c["temps"])
     f = seqs[0][1][0]
     cam = R.orbit_camera((2.75, 0.42, 0.0), 2.3, 0.3, 7.6, 1280 / 720)
     outs = []
@@ -81,7 +85,7 @@ def test_render_full_size_deterministic(setup):
 def test_render_errors(setup):
     from windtunnel import WindTunnelError
     from windtunnel import render as R
-    mc, mr, z, e, seqs = setup
+    mc, mr, z, e, seqs, shape, c = setup
     r = R.Renderer(e, 16, 8)
     f = seqs[0][1][0]
     lk = f["look"]

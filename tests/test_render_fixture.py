@@ -27,7 +27,8 @@ def test_fixture_is_consistent():
     import make_render as mr
     z = fixture()
     keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
-    assert keys == ["hero_0", "hero_1", "slice-x_0", "slice-y_0", "slice-z_0", "surface_0"]
+    assert keys == ["cube_0", "empty_0", "hero_0", "hero_1", "slice-x_0", "slice-y_0", "slice-z_0", "sphere_0",
+                    "surface_0", "wing_0"]
     for k in keys:
         sc, out = z[k + "_scene"].astype(np.float32), z[k + "_out"]
         assert sc.shape == (mr.H, mr.W, 4) and out.shape == (mr.H, mr.W, 4) and out.dtype == np.uint8
@@ -56,8 +57,8 @@ def test_reference_reproduces_fixture():
         hist = [np.zeros((mr.H, mr.W, 4), np.float32) for _ in range(2)]
         for k, f in enumerate(frames):
             u = mr.frame_uniforms(st, f)
-            scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, c["fields"], c["temps"], shape, u.cam,
-                                              f["look"], mc.view(), mr.W, mr.H)
+            scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, c["fields"], c["temps"],
+                                              mr.frame_shape(shape, f), u.cam, f["look"], mc.view(), mr.W, mr.H)
             hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)
             glow = pyoracle.ref_glow(scene, f.get("parts"), u.pdraw, f.get("lines"), u.sdraw)
             bb = pyoracle.ref_blur(pyoracle.ref_blur(glow, (1.0, 0.0), 3.0, 1.0, mr.W // 2, mr.H // 2), (0.0, 1.0),

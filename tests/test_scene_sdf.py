@@ -82,8 +82,8 @@ def test_device_render_pixel_matches_fixture(hm):
         for k, f in enumerate(frames):
             u = mr.frame_uniforms(st, f)
             from oracle import pyoracle
-            out = pyoracle.shade_model_render(shape, u.cam, f["look"], view, dims, org, mc.H, c["fields"], c["temps"],
-                                              mr.W, mr.H, threads=4)
+            out = pyoracle.shade_model_render(mr.frame_shape(shape, f), u.cam, f["look"], view, dims, org, mc.H,
+                                              c["fields"], c["temps"], mr.W, mr.H, threads=4)
             ref = z[f"{name}_{k}_scene"]
             bad = np.argwhere(np.any(out.astype(np.float16).view(np.uint16) != ref.view(np.uint16), axis=-1))
             assert len(bad) == 0, f"{name}_{k}: {len(bad)} pixels differ, first {bad[:4].tolist()}"
