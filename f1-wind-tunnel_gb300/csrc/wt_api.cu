@@ -81,6 +81,11 @@ struct wt_ctx {
   };
   std::vector<Graph> graphs;               // captured wt_step sequences
   wt_shape shape{WT_KIND_EMPTY};           // last voxelized shape (the renderer's scene)
+  // the baked W17 model (wt_set_car_model): device copies
+  uint16_t* car_body = nullptr;
+  uint16_t* car_parts = nullptr;
+  float4* car_rig = nullptr;
+  uint32_t car_pdims[3] = {1, 1, 1};
   std::vector<wt_renderer*> renderers;     // live renderers over this lattice
   std::string err;
 };
@@ -502,7 +507,7 @@ int wt_destroy(wt_ctx* c) {
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
                   c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters,
-                  c->hist_pos, c->d_reduce};
+                  c->hist_pos, c->d_reduce, c->car_body, c->car_parts, c->car_rig};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);
@@ -537,16 +542,64 @@ int wt_reset(wt_ctx* c) {
   return WT_OK;
 }
 
+CarView car_view(const wt_ctx* c) {
+  CarView v;
+  v.body = c->car_body;
+  v.parts = c->car_parts;
+  for (int i = 0; i < 3; i++) v.pdims[i] = c->car_pdims[i];
+  v.rig = c->car_rig;
+  return v;
+}
+
+int wt_set_car_model(wt_ctx* c, const uint16_t* body, const uint16_t* parts, const uint32_t parts_dims[3],
+                     const wt_rig* rig) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!body || !parts || !parts_dims || !rig) return fail(c, WT_ERR_ARG, "wt_set_car_model: null argument");
+  const uint64_t np = (uint64_t)parts_dims[0] * parts_dims[1] * parts_dims[2];
+  if (np == 0 || parts_dims[0] > 4096 || parts_dims[1] > 4096 || parts_dims[2] > 4096)
+    return fail(c, WT_ERR_ARG, "wt_set_car_model: parts atlas dimensions must be 1..4096");
+  static_assert(sizeof(wt_rig) == 87 * 16, "wt_rig is the 87 vec4 of the Rig uniform");
+  const size_t nb = (size_t)368 * 84 * 67;
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));  // earlier work may still read the old model
+  uint16_t* b = nullptr;
+  uint16_t* pa = nullptr;
+  float4* rg = nullptr;
+  cudaError_t e = cudaMalloc((void**)&b, nb * 2);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&pa, np * 2);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&rg, sizeof(wt_rig));
+  if (e == cudaSuccess) e = cudaMemcpy(b, body, nb * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(pa, parts, np * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(rg, rig, sizeof(wt_rig), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(b);
+    cudaFree(pa);
+    cudaFree(rg);
+    return fail(c, e == cudaErrorMemoryAllocation ? WT_ERR_NOMEM : WT_ERR_CUDA,
+                std::string("wt_set_car_model: ") + cudaGetErrorString(e));
+  }
+  cudaFree(c->car_body);
+  cudaFree(c->car_parts);
+  cudaFree(c->car_rig);
+  c->car_body = b;
+  c->car_parts = pa;
+  c->car_rig = rg;
+  for (int i = 0; i < 3; i++) c->car_pdims[i] = parts_dims[i];
+  return WT_OK;
+}
+
 int wt_voxelize(wt_ctx* c, const wt_shape* shape) {
   int rc = check_ctx(c);
   if (rc) return rc;
   if (!shape) return fail(c, WT_ERR_ARG, "wt_voxelize: null shape");
   const uint32_t k = shape->kind;
   if (!(k == WT_KIND_F1 || k == WT_KIND_SPHERE || k == WT_KIND_CUBE || k == WT_KIND_WING || k == WT_KIND_EMPTY ||
-        k == WT_KIND_BOX))
+        k == WT_KIND_BOX || k == WT_KIND_W17))
     return fail(c, WT_ERR_UNSUPPORTED, "wt_voxelize: scene kind " + std::to_string(k) +
-                                           " is not built (custom profile and baked-mesh scenes)");
-  WT_CUDA(c, launch_voxelize(*shape, c->grid, c->solid, c->emit, c->stream));
+                                           " is not built (custom profile scene)");
+  if (k == WT_KIND_W17 && !c->car_body)
+    return fail(c, WT_ERR_STATE, "wt_voxelize: the W17 scene needs a car model (wt_set_car_model)");
+  WT_CUDA(c, launch_voxelize(*shape, car_view(c), c->grid, c->solid, c->emit, c->stream));
   c->shape = *shape;
   return rebuild_links(c);
 }
@@ -1353,6 +1406,7 @@ int wt_render_scene(wt_renderer* r, const wt_cam* cam, const wt_look* look, cons
     return fail(c, WT_ERR_UNSUPPORTED, "wt_render_scene: the baked-mesh G-buffer path (mesh_mode) is not built");
   SceneArgs a;
   a.shape = c->shape;
+  a.car = car_view(c);
   a.g = field_grid(c);
   a.view = view_args(view);
   a.pos = f3(cam->pos); a.fwd = f3(cam->fwd); a.right = f3(cam->right); a.up = f3(cam->up);

@@ -121,7 +121,15 @@ cudaError_t launch_resample_init(uint32_t storage, const float4* coarse, uint32_
                                  uint64_t np, cudaStream_t s);
 
 // wt_voxel.cu
-cudaError_t launch_voxelize(const wt_shape& shape, const wt_grid& grid, uint8_t* solid, float* emit,
+// The baked W17 model's device buffers (wt_set_car_model); empty = no model.
+struct CarView {
+  const uint16_t* body = nullptr;   // 368 x 84 x 67 binary16 body distances, x fastest
+  const uint16_t* parts = nullptr;  // parts atlas, pdims[0] x [1] x [2] binary16, x fastest
+  uint32_t pdims[3] = {1, 1, 1};
+  const float4* rig = nullptr;      // the Rig uniform: front[71], hinges, angles, extra, fly, grids[12]
+};
+
+cudaError_t launch_voxelize(const wt_shape& shape, const CarView& car, const wt_grid& grid, uint8_t* solid, float* emit,
                             cudaStream_t s);
 cudaError_t launch_sdf_sample(const wt_shape& shape, const wt_grid& grid, float* out, cudaStream_t s);
 cudaError_t launch_cell_words(const uint8_t* solid, const float* emit, uint32_t* cellw, uint32_t nx, uint32_t ny,

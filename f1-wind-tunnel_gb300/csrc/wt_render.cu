@@ -392,7 +392,7 @@ dim3 tiles(uint32_t w, uint32_t h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h
 }  // namespace
 
 cudaError_t launch_render_scene(const SceneArgs& a, cudaStream_t s) {
-  const Scene S = make_scene(a.shape);
+  const Scene S = make_scene(a.shape, a.car);
   const dim3 b(8, 8);
   scene_kernel<<<tiles(a.w, a.h, b), b, 0, s>>>(S, a);
   return cudaGetLastError();

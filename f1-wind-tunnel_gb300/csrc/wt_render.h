@@ -18,6 +18,7 @@ struct F3 {
 
 struct SceneArgs {
   wt_shape shape;             // the context's shape (Shape uniform)
+  CarView car;                // its W17 model, if any
   FieldGrid g;                // fields / temperatures of the last step call
   ViewArgs view;
   // Cam (render-wgsl.ts:5-11)

@@ -7,6 +7,8 @@
 // direction) are computed once on the host by make_scene with the same
 // functions, which gives the same bits as evaluating them per point.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "wt_fmath.h"
 #include "wt_internal.h"
 #include "wt_vec.cuh"
@@ -17,6 +19,7 @@ namespace {
 // Shape plus host-computed shape-wide constants.
 struct Scene {
   wt_shape s;
+  CarView car;                // the W17 model (kind 5)
   float rake_c, rake_s;       // cos/sin of the rake angle (f1.ts:37-40)
   float rear_c, rear_s;       // cos/sin of the rear main-plane angle after variant offsets (f1.ts:274)
   float ang_m, ang_f, chord_m, chord_f, rise_m, ep_hx, ep_hy;  // rear-wing variant (f1.ts:260-272)
@@ -320,12 +323,176 @@ __device__ float f1_emission(const Scene& S, V3 pw) {
   if (p.x > 3.55f && p.x < 4.25f && p.z < 0.13f && p.y > b + 0.42f) e = mx(e, S.s.heat_rad * 1.4f);
   return e;
 }
+
+// ---------------------------------------------------------------- baked W17 model (kind 5)
+// src/engine/f1.ts:322-394 and the rig functions of src/engine/car-model.ts:59-136.
+constexpr float W17_H = 0.015f, W17_BASE_RIDE = 0.092f;
+constexpr int RIG_HINGES = 71, RIG_ANGLES = 72, RIG_EXTRA = 73, RIG_FLY = 74, RIG_GRIDS = 75;
+
+__device__ __forceinline__ float4 rig_at(const Scene& S, int i) { return __ldg(S.car.rig + i); }
+__device__ __forceinline__ float half_at(const uint16_t* t, size_t i) {
+  return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(t) + i)));
+}
+// textureSampleLevel of an r16float texture through the engine's linear,
+// clamp-to-edge sampler (engine.ts:270) with f32 weights: c = uvw * size - 0.5,
+// i = floor(c), t = c - i, clamped indices, blended along x, then y, then z.
+__device__ __forceinline__ int floor_index(float f, int n) { return (int)(f < -1.0f ? -1.0f : (f > (float)n ? (float)n : f)); }
+__device__ float sample3(const uint16_t* tex, int w, int h, int d, V3 uvw) {
+  const float cx = uvw.x * (float)w - 0.5f, cy = uvw.y * (float)h - 0.5f, cz = uvw.z * (float)d - 0.5f;
+  const float fx = floorf(cx), fy = floorf(cy), fz = floorf(cz);
+  const float tx = cx - fx, ty = cy - fy, tz = cz - fz;
+  const int i = floor_index(fx, w), j = floor_index(fy, h), k = floor_index(fz, d);
+  auto at = [&](int x, int y, int z) {
+    x = x < 0 ? 0 : (x >= w ? w - 1 : x);
+    y = y < 0 ? 0 : (y >= h ? h - 1 : y);
+    z = z < 0 ? 0 : (z >= d ? d - 1 : z);
+    return half_at(tex, ((size_t)z * (size_t)h + (size_t)y) * (size_t)w + (size_t)x);
+  };
+  const float c00 = at(i, j, k) * (1.0f - tx) + at(i + 1, j, k) * tx;
+  const float c10 = at(i, j + 1, k) * (1.0f - tx) + at(i + 1, j + 1, k) * tx;
+  const float c01 = at(i, j, k + 1) * (1.0f - tx) + at(i + 1, j, k + 1) * tx;
+  const float c11 = at(i, j + 1, k + 1) * (1.0f - tx) + at(i + 1, j + 1, k + 1) * tx;
+  const float c0 = c00 * (1.0f - ty) + c10 * ty, c1 = c01 * (1.0f - ty) + c11 * ty;
+  return c0 * (1.0f - tz) + c1 * tz;
+}
+
+// rigWeight, rigHinge, rigAngle, rigScale, rigRotate (car-model.ts:70-118); the
+// RIG constants (car-model.ts:44-49) as the reference interpolates them
+__device__ float rig_weight(uint32_t part, float z) {
+  if (part == 1u || part == 2u) {
+    const float az = ab(z);
+    return sstep(0.16f, 0.22f, az) * (1.0f - sstep(0.5f, 0.56f, az));
+  }
+  return (part == 3u || part == 4u) ? 1.0f : 0.0f;
+}
+__device__ V2 rig_hinge(const Scene& S, uint32_t part, float z) {
+  if (part == 3u) { const float4 g = rig_at(S, RIG_HINGES); return v2(g.z, g.w); }
+  if (part == 4u) { const float4 g = rig_at(S, RIG_HINGES); return v2(g.x, g.y); }
+  const float f = clmp(ab(z) / 0.01f, 0.0f, 70.0f);
+  const uint32_t i = (uint32_t)floorf(f);
+  const uint32_t j = (i + 1u) < 70u ? i + 1u : 70u;
+  const float4 a = rig_at(S, (int)i), b = rig_at(S, (int)j);
+  const float t = f - (float)i;
+  return part == 1u ? mix2(v2(a.x, a.y), v2(b.x, b.y), t) : mix2(v2(a.z, a.w), v2(b.z, b.w), t);
+}
+__device__ float rig_angle(const Scene& S, uint32_t part, float z) {
+  const float4 an = rig_at(S, RIG_ANGLES);
+  float a = 0.0f;
+  if (part == 1u) a = an.x;
+  else if (part == 2u) a = an.y;
+  else if (part == 3u) a = an.z;
+  else if (part == 4u) a = an.w;
+  if (part == 3u || part == 4u) a = a + rig_at(S, RIG_EXTRA).x * sstep(0.12f, 0.48f, ab(z));
+  return a * rig_weight(part, z);
+}
+__device__ float rig_scale(const Scene& S, uint32_t part) {
+  const float ey = rig_at(S, RIG_EXTRA).y;
+  if (part == 3u) return ey;
+  if (part == 1u || part == 2u) return 1.0f - (1.0f - ey) * 0.65f;
+  return 1.0f;
+}
+// rigRotate with dir = -1 (the distance field's direction)
+__device__ V3 rig_rotate_back(const Scene& S, V3 p, uint32_t part) {
+  if (part == 0u || part > 4u) return p;
+  const float a = rig_angle(S, part, p.z) * -1.0f;
+  const float k = rig_scale(S, part);
+  const V2 h = rig_hinge(S, part, p.z);
+  const float c = wtm::cosf(a), s = wtm::sinf(a);
+  V2 d = v2(p.x, p.y) - h;
+  d = v2(c * d.x - s * d.y, s * d.x + c * d.y);
+  d = v2(dv(d.x, k), dv(d.y, k));
+  return v3(h.x + d.x, h.y + d.y, p.z);
+}
+// podWeight, podDeform (car-model.ts:121-135), dir = -1
+__device__ float pod_weight(V3 p) {
+  return sstep(1.85f, 2.25f, p.x) * (1.0f - sstep(3.55f, 4.05f, p.x)) * sstep(0.12f, 0.2f, p.y) *
+         (1.0f - sstep(0.6f, 0.7f, p.y)) * sstep(0.26f, 0.4f, ab(p.z));
+}
+__device__ V3 pod_deform_back(const Scene& S, V3 p) {
+  const float c = rig_at(S, RIG_EXTRA).z * pod_weight(p);
+  if (c <= 0.0f) return p;
+  const float az = ab(p.z);
+  const float kz = dv(1.0f, 1.0f - c);
+  const float ky = dv(1.0f, 1.0f - 0.45f * c);
+  const float nz = az > 0.26f ? 0.26f + (az - 0.26f) * kz : az;
+  const float sg = p.z > 0.0f ? 1.0f : (p.z < 0.0f ? -1.0f : 0.0f);
+  return v3(p.x, 0.12f + (p.y - 0.12f) * ky, sg * nz);
+}
+// w17BodyFrame (f1.ts:329-334), with the rake of toBodyFrame
+__device__ V3 w17_body_frame(const Scene& S, V3 pw) {
+  const float dx = pw.x - FA, dy = pw.y - S.s.ride_h;
+  return v3(FA + dx * S.rake_c + dy * S.rake_s, W17_BASE_RIDE - dx * S.rake_s + dy * S.rake_c, pw.z);
+}
+// sdW17Body (f1.ts:335-341)
+__device__ float sd_w17_body(const Scene& S, V3 p) {
+  const V3 ext = v3(368.0f * W17_H, 84.0f * W17_H, 67.0f * W17_H);
+  const V3 half = ext * 0.5f;
+  const float box = sd_box(p - v3(-0.3f + half.x, 0.0f + half.y, 0.0f + half.z), half);
+  if (box > 0.0f) return box + 0.07f;
+  const V3 uvw = v3(dv(dv(p.x - -0.3f, W17_H) + 0.5f, 368.0f), dv(dv(p.y - 0.0f, W17_H) + 0.5f, 84.0f),
+                    dv(dv(p.z - 0.0f, W17_H) + 0.5f, 67.0f));
+  return sample3(S.car.body, 368, 84, 67, uvw);
+}
+// sdW17Part (f1.ts:342-353)
+__device__ __noinline__ float sd_w17_part(const Scene& S, V3 pb, uint32_t part) {
+  const float4 g0 = rig_at(S, RIG_GRIDS + (int)(part - 1u) * 2), g1 = rig_at(S, RIG_GRIDS + (int)(part - 1u) * 2 + 1);
+  const V3 q = rig_rotate_back(S, pb, part);
+  const V3 ext = v3((g1.x - 1.0f) * g0.w, (g1.y - 1.0f) * g0.w, (g1.z - 1.0f) * g0.w);
+  const V3 half = ext * 0.5f;
+  const float box = sd_box(q - v3(g0.x + half.x, g0.y + half.y, g0.z + half.z), half);
+  if (box > 0.0f) return box + 0.03f;
+  const V3 cell = v3(dv(q.x - g0.x, g0.w), dv(q.y - g0.y, g0.w), dv(q.z - g0.z, g0.w));
+  const float ax = (float)S.car.pdims[0], ay = (float)S.car.pdims[1], az = (float)S.car.pdims[2];
+  const V3 uvw = v3(dv(cell.x + 0.5f, ax), dv(cell.y + 0.5f, ay), dv(cell.z + g1.w + 0.5f, az));
+  const float sc = rig_scale(S, part);
+  return sample3(S.car.parts, (int)S.car.pdims[0], (int)S.car.pdims[1], (int)S.car.pdims[2], uvw) * mn(sc, 1.0f);
+}
+// sdW17 (f1.ts:354-369)
+__device__ V2 sd_w17(const Scene& S, V3 pw) {
+  const V3 pa = v3(pw.x, pw.y, ab(pw.z));
+  const V3 p = w17_body_frame(S, pa);
+  const float squeeze = 1.0f - rig_at(S, RIG_EXTRA).z * pod_weight(p);
+  V2 res = v2(sd_w17_body(S, pod_deform_back(S, p)) * 0.95f * squeeze, 12.0f);
+  const float4 fly = rig_at(S, RIG_FLY);
+  if (fly.z > 0.5f && p.x < 0.85f && p.y < 0.6f)
+    res = op_u(res, v2(mn(mn(sd_w17_part(S, p, 1u), sd_w17_part(S, p, 2u)), sd_w17_part(S, p, 5u)) * 0.95f, 7.0f));
+  if (fly.w > 0.5f && p.x > 4.4f && p.y > 0.5f)
+    res = op_u(res, v2(mn(mn(sd_w17_part(S, p, 3u), sd_w17_part(S, p, 4u)), sd_w17_part(S, p, 6u)) * 0.95f, 8.0f));
+  const V3 front = v3(1.0f, 0.36f, 0.779f), rear = v3(4.4f, 0.351f, 0.737f);
+  res = op_u(res, v2(mn(sd_tyre(pa, front, 0.175f), sd_cyl_z(pa - front, 0.234f, 0.15f)), 2.0f));
+  res = op_u(res, v2(mn(sd_tyre(pa, rear, 0.205f), sd_cyl_z(pa - rear, 0.234f, 0.18f)), 2.0f));
+  return res;
+}
+// w17Duct (f1.ts:374-383)
+__device__ float w17_duct(const Scene& S, V3 pw) {
+  if (S.s.duct <= 0.0f) return 1e3f;
+  const V3 p = pod_deform_back(S, w17_body_frame(S, v3(pw.x, pw.y, ab(pw.z))));
+  const float k = S.s.duct;
+  const float mouth = sd_capsule(p, v3(2.05f, 0.52f, 0.58f), v3(3.0f, 0.50f, 0.48f), 0.09f * k);
+  const float main = sd_capsule(p, v3(2.05f, 0.55f, 0.47f), v3(3.25f, 0.46f, 0.43f), 0.1f * k);
+  const float exit = sd_capsule(p, v3(3.25f, 0.46f, 0.43f), v3(4.1f, 0.40f, 0.32f), 0.085f * k);
+  return mn(mn(mouth, main), exit);
+}
+// w17Emission (f1.ts:386-394)
+__device__ float w17_emission(const Scene& S, V3 pw) {
+  const V3 pa = v3(pw.x, pw.y, ab(pw.z));
+  const V3 p = w17_body_frame(S, pa);
+  float e = 0.0f;
+  if (len2(v2(pa.x - 1.0f, pa.y - 0.36f)) < 0.2f && ab(pa.z - (0.779f - 0.215f)) < 0.1f) e = mx(e, S.s.heat_brakes);
+  if (len2(v2(pa.x - 4.4f, pa.y - 0.351f)) < 0.2f && ab(pa.z - (0.737f - 0.245f)) < 0.1f) e = mx(e, S.s.heat_brakes * 0.8f);
+  if (len3(p - v3(5.07f, 0.53f, 0.0f)) < 0.1f) e = mx(e, S.s.heat_engine);
+  if (p.x > 3.7f && p.x < 4.3f && p.y > 0.2f && p.y < 0.5f && p.z > 0.18f && p.z < 0.48f) e = mx(e, S.s.heat_rad);
+  if (p.x > 4.15f && p.x < 4.65f && p.y > 0.5f && p.z < 0.16f) e = mx(e, S.s.heat_rad * 1.4f);
+  return e;
+}
+
 __device__ V2 scene_sdf(const Scene& S, V3 p) {
   switch (S.s.kind) {
     case WT_KIND_F1: return sd_f1(S, p);
     case WT_KIND_SPHERE: return v2(len3(p - v3(2.6f, 1.0f, 0.0f)) - 0.6f, 6.0f);
     case WT_KIND_CUBE: return v2(sd_rbox(p - v3(2.6f, 1.0f, 0.0f), v3(0.5f, 0.5f, 0.5f), 0.03f), 6.0f);
     case WT_KIND_WING: return v2(sd_wing(p, v2(1.6f, 1.2f), 1.8f, -S.s.aoa, 0.24f, -1.25f, 1.25f), 6.0f);
+    case WT_KIND_W17: return S.car.body ? sd_w17(S, p) : v2(1e3f, 0.0f);
     case WT_KIND_BOX:
       return v2(sd_box(p - v3(S.s.box_center[0], S.s.box_center[1], S.s.box_center[2]),
                        v3(S.s.box_half[0], S.s.box_half[1], S.s.box_half[2])), 6.0f);
@@ -334,9 +501,10 @@ __device__ V2 scene_sdf(const Scene& S, V3 p) {
 }
 
 // Shape plus its shape-wide constants.
-Scene make_scene(const wt_shape& shape) {
+Scene make_scene(const wt_shape& shape, const CarView& car = CarView{}) {
   Scene S;
   S.s = shape;
+  S.car = car;
   // Shape-wide constants, evaluated once (same functions and operation order as per cell).
   const float th = wtm::atanf((shape.rear_ride - shape.ride_h) / (RA26 - FA));
   S.rake_c = wtm::cosf(th);

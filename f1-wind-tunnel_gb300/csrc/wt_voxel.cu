@@ -30,13 +30,19 @@ __global__ void voxelize_kernel(Scene S, uint32_t nx, uint32_t ny, uint32_t nz, 
   if (x >= nx || y >= ny) return;
   const uint32_t idx = x + nx * (y + ny * z);
   const V3 p = v3(ox + ((float)x + 0.5f) * h, oy + ((float)y + 0.5f) * h, oz + ((float)z + 0.5f) * h);
-  const V2 r = scene_sdf(S, p);
-  const bool inside = r.x < 0.3f * h && x > 1u && x < nx - 2u;
+  V2 r = scene_sdf(S, p);
+  const bool w17 = S.s.kind == WT_KIND_W17 && S.car.body != nullptr;
+  // the W17's cooling ducts are carved out of its body (wgsl.ts:313) and marked
+  // with emission -1 (wgsl.ts:319-320): the step relaxes the air there
+  const float duct = w17 ? w17_duct(S, p) : 1e3f;
+  if (w17 && ab(r.y - 12.0f) < 0.5f) r.x = mx(r.x, -duct);
+  const bool inside = r.x < (w17 ? 0.45f : 0.3f) * h && x > 1u && x < nx - 2u;
   uint32_t group = 1u;
   if (ab(r.y - 7.0f) < 0.5f) group = 2u;
   if (ab(r.y - 8.0f) < 0.5f) group = 3u;
   solid[idx] = inside ? (uint8_t)group : (uint8_t)0;
-  emit[idx] = inside ? (S.s.kind == WT_KIND_F1 ? f1_emission(S, p) : 0.0f) : 0.0f;
+  const float em = S.s.kind == WT_KIND_F1 ? f1_emission(S, p) : (w17 ? w17_emission(S, p) : 0.0f);
+  emit[idx] = inside ? em : (w17 && duct < 0.0f ? -1.0f : 0.0f);
 }
 
 // ---------------------------------------------------------------- cell words
@@ -142,8 +148,9 @@ cudaError_t launch_sdf_sample(const wt_shape& shape, const wt_grid& grid, float*
   return cudaGetLastError();
 }
 
-cudaError_t launch_voxelize(const wt_shape& shape, const wt_grid& grid, uint8_t* solid, float* emit, cudaStream_t s) {
-  const Scene S = make_scene(shape);
+cudaError_t launch_voxelize(const wt_shape& shape, const CarView& car, const wt_grid& grid, uint8_t* solid, float* emit,
+                            cudaStream_t s) {
+  const Scene S = make_scene(shape, car);
   const dim3 block(32, 4, 1);
   const dim3 g((grid.nx + 31) / 32, (grid.ny + 3) / 4, grid.nz);
   voxelize_kernel<<<g, block, 0, s>>>(S, grid.nx, grid.ny, grid.nz, grid.origin[0], grid.origin[1], grid.origin[2],

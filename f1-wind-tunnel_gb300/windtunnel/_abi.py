@@ -22,7 +22,7 @@ ERRORS = {
 }
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 STORAGE = {"f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
-KIND_F1, KIND_SPHERE, KIND_CUBE, KIND_WING, KIND_EMPTY, KIND_BOX = 0, 1, 2, 3, 6, 7
+KIND_F1, KIND_SPHERE, KIND_CUBE, KIND_WING, KIND_W17, KIND_EMPTY, KIND_BOX = 0, 1, 2, 3, 5, 6, 7
 
 
 class WindTunnelError(RuntimeError):
@@ -189,6 +189,7 @@ _PROTOS = {
     "wt_sample_flow": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp, _vp]),
     "wt_particles_step": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(PSim), ctypes.POINTER(View)]),
     "wt_streamlines": (ctypes.c_int, [_vp, ctypes.POINTER(StreamParams), ctypes.POINTER(View), _vp]),
+    "wt_set_car_model": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "wt_render_create": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_vp)]),
     "wt_render_destroy": (None, [_vp]),
     "wt_render_scene": (ctypes.c_int, [_vp, ctypes.POINTER(Cam), ctypes.POINTER(Look), ctypes.POINTER(View)]),

@@ -213,6 +213,18 @@ class AeroEngine:
         self.shape_params = p
         self.set_shape_raw(pack_shape(p))
 
+    def set_car_model(self, model):
+        """setCarModel (engine.ts:410-421) with its rig: a car_model.CarModel
+        (body SDF, parts atlas, Rig uniform) for scene kind ShapeKind.W17."""
+        body = np.ascontiguousarray(model.body_sdf, np.uint16)
+        parts = np.ascontiguousarray(model.parts, np.uint16)
+        dims = np.array(model.parts_dims, np.uint32)
+        rig = np.ascontiguousarray(model.rig, np.float32)
+        assert body.size == 368 * 84 * 67 and parts.size == int(np.prod(dims)) and rig.shape == (87, 4)
+        self._check(self.lib.wt_set_car_model(self.ctx, body.ctypes.data, parts.ctypes.data, dims.ctypes.data,
+                                              rig.ctypes.data), "wt_set_car_model")
+        self.car_model = model
+
     def set_shape_raw(self, shape: _abi.Shape):
         self._check(self.lib.wt_voxelize(self.ctx, ctypes.byref(shape)), "wt_voxelize")
 

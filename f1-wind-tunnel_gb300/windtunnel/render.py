@@ -97,6 +97,8 @@ def shape_bounds(params):
     k = params.kind if params is not None else ShapeKind.Empty
     if k == ShapeKind.F1:
         return (-0.08, 0.0, -0.98), (5.46, params.rideH + 1.34, 0.98)
+    if k == ShapeKind.W17:
+        return (-0.3, 0.0, -0.98), (5.2, params.rideH + 1.16, 0.98)
     if k == ShapeKind.Sphere:
         return (1.95, 0.35, -0.65), (3.25, 1.65, 0.65)
     if k == ShapeKind.Cube:

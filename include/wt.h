@@ -50,6 +50,7 @@ extern "C" {
 #define WT_KIND_SPHERE 1u /* wgsl.ts:104 */
 #define WT_KIND_CUBE 2u   /* wgsl.ts:105, 1 m rounded cube at (2.6, 1.0, 0) */
 #define WT_KIND_WING 3u   /* wgsl.ts:106 */
+#define WT_KIND_W17 5u    /* baked W17 model, src/engine/f1.ts:322-381; needs wt_set_car_model */
 #define WT_KIND_EMPTY 6u  /* wgsl.ts:108 */
 #define WT_KIND_BOX 7u    /* build extension: axis-aligned box box_center +- box_half */
 
@@ -130,6 +131,27 @@ int wt_set_sim(wt_ctx* ctx, const wt_sim* sim);
 /* reset() (engine.ts:371-381, LBM_INIT wgsl.ts:147-155): populations to
  * feq(1, (u_in,0,0)), fields to (u_in,0,0,1), temperatures to 0.  Keeps the scene. */
 int wt_reset(wt_ctx* ctx);
+
+/* Rig uniform of the baked W17 model (src/engine/car-model.ts:60-69): the
+ * articulated wing elements' hinges, angles, extras and part grids. */
+typedef struct wt_rig {
+  float front[71][4];  /* front flap hinges along |z| in 1 cm bins: flap A xy, flap B zw */
+  float hinges[4];     /* rear main plane xy, rear flap zw */
+  float angles[4];     /* front flap A, front flap B, rear flap, rear main plane (rad) */
+  float extra[4];      /* rear tip twist (rad), flap chord scale, sidepod squeeze, unused */
+  float fly[4];        /* fly-away progress front / rear, fitted front / rear (1 or 0) */
+  float grids[12][4];  /* per part (6): origin xyz + cell size, dims xyz + atlas z offset */
+} wt_rig;
+
+/* setCarModel (engine.ts:410-421) plus the rig of setShape (engine.ts:450-462):
+ * the W17 model that scene kind WT_KIND_W17 voxelizes and renders.  body_sdf:
+ * 368 x 84 x 67 binary16 distances at 1.5 cm from (-0.3, 0, 0), x fastest;
+ * parts: the atlas of per-part grids (partsAtlas, car-model.ts:176-193),
+ * parts_dims[0] x [1] x [2] binary16, x fastest.  Copied to the device; a later
+ * call replaces the model (call it again with a new rig when the wing settings
+ * change).  Sampling is trilinear with clamp-to-edge, in f32. */
+int wt_set_car_model(wt_ctx* ctx, const uint16_t* body_sdf, const uint16_t* parts, const uint32_t parts_dims[3],
+                     const wt_rig* rig);
 
 /* setShape() (engine.ts:426-470, VOXELIZE wgsl.ts:305-321): voxelize the scene
  * into solid flags, heat emission and bounce-back link masks.  Populations are

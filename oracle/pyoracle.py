@@ -79,6 +79,7 @@ def _load_ref():
     L.wtr_present.argtypes = [_vp, _i, _i, _vp, _i, _i, _vp, _i, _i, _vp, _vp]
     L.wtr_glow.argtypes = [_vp, _i, _i, _vp, _vp, ctypes.c_uint32, _vp, _vp, ctypes.c_uint32, _vp]
     L.wtr_scene_sdf.argtypes = [_vp, _vp, ctypes.c_uint32, _vp]
+    L.wtr_set_car.argtypes = [_vp, _vp, _vp, _vp]
     return L
 
 
@@ -97,8 +98,26 @@ def shade_model_lib():
         L = ctypes.CDLL(SHADE_SO)
         L.wthm_render.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _F, _vp, _vp] + [ctypes.c_uint32] * 4 + [_vp]
         L.wthm_scene_sdf.argtypes = [_vp, _vp, ctypes.c_uint32, _vp]
+        L.wthm_set_car.argtypes = [_vp, _vp, _vp, _vp]
         _S = L
     return _S
+
+
+_SCAR = None
+
+
+def shade_model_set_car(car):
+    """Bind a W17 model (windtunnel.car_model.CarModel) to the host-built shading code, or None."""
+    global _SCAR
+    L = shade_model_lib()
+    if car is None:
+        L.wthm_set_car(None, None, None, None)
+        _SCAR = None
+        return
+    keep = (np.ascontiguousarray(car.body_sdf, np.uint16), np.ascontiguousarray(car.parts, np.uint16),
+            np.array(car.parts_dims, np.uint32), np.ascontiguousarray(car.rig, np.float32))
+    L.wthm_set_car(*(a.ctypes.data for a in keep))
+    _SCAR = keep
 
 
 def shade_model_render(shape, cam, look, view, dims, origin, h, fields, temps, width, height, threads=1, rows=None):
@@ -219,6 +238,26 @@ def ref_scene_sdf(shape, pts):
     out = np.zeros((p.shape[0], 2), np.float32)
     L.wtr_scene_sdf(w.ctypes.data, p.ctypes.data, p.shape[0], out.ctypes.data)
     return out
+
+
+_CAR = None
+
+
+def ref_set_car(car):
+    """Bind a W17 model (windtunnel.car_model.CarModel: body SDF, parts atlas, rig)
+    to the translated reference, or unbind it with None."""
+    global _CAR
+    L = ref_lib()
+    if car is None:
+        L.wtr_set_car(None, None, None, None)
+        _CAR = None
+        return
+    sdf = np.ascontiguousarray(car.body_sdf, np.uint16)
+    parts = np.ascontiguousarray(car.parts, np.uint16)
+    dims = np.array(car.parts_dims, np.uint32)
+    rig = np.ascontiguousarray(car.rig, np.float32).reshape(87, 4)
+    L.wtr_set_car(sdf.ctypes.data, parts.ctypes.data, dims.ctypes.data, rig.ctypes.data)
+    _CAR = (sdf, parts, dims, rig)
 
 
 def ref_taa(cur, hist, taa):

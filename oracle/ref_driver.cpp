@@ -58,13 +58,42 @@ void set_shape(S& s, const uint32_t* w) {
   s.cover = f[20]; s.nose = f[21]; s.rearRide = f[22]; s.duct = f[23];
 }
 
-// Rig uniform as the engine creates it before any W17 model is loaded (engine.ts:273-277).
+// The W17 model set by wtr_set_car (engine.ts:410-421 setCarModel + the rig of
+// setShape, :450-462); absent until set.
+struct CarModel {
+  std::vector<uint16_t> sdf, parts;
+  int pdims[3] = {1, 1, 1};
+  float rig[87 * 4];
+  bool set = false;
+};
+CarModel g_car;
+
+// Rig uniform: the car model's, or as the engine creates it before any W17
+// model is loaded (engine.ts:273-277).
 template <class R>
 void set_rig(R& rig) {
   rig = R{};
+  if (g_car.set) {
+    const float* f = g_car.rig;
+    auto v4 = [&](int i) { return rt::vec4f(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]); };
+    for (int i = 0; i < 71; i++) rig.front[i] = v4(i);
+    rig.hinges = v4(71); rig.angles = v4(72); rig.extra = v4(73); rig.fly = v4(74);
+    for (int i = 0; i < 12; i++) rig.grids[i] = v4(75 + i);
+    return;
+  }
   rig.extra = rt::vec4f(0.0f, 1.0f, 0.0f, 0.0f);
   rig.fly = rt::vec4f(0.0f, 0.0f, 1.0f, 1.0f);
   for (int i = 0; i < 12; i++) rig.grids[i] = rt::vec4f(0.0f, 0.0f, 0.0f, 1.0f);
+}
+template <class M>
+void set_car_textures(M& carSdf, M& carParts) {
+  if (g_car.set) {
+    carSdf = rt::texture3d{368, 84, 67, g_car.sdf.data()};
+    carParts = rt::texture3d{g_car.pdims[0], g_car.pdims[1], g_car.pdims[2], g_car.parts.data()};
+  } else {
+    carSdf = rt::texture3d{};
+    carParts = rt::texture3d{};
+  }
 }
 
 template <class G>
@@ -151,6 +180,7 @@ void wtr_voxelize(void* p, const uint32_t* w) {
   set_grid(M::grid, *r);
   set_shape(M::shape, w);
   set_rig(M::rig);
+  set_car_textures(M::carSdf, M::carParts);
   M::profile.p = r->profile.data();
   M::solid.p = r->solid.data();
   M::emit.p = r->emit.data();
@@ -335,6 +365,7 @@ void wtr_render_scene(const uint32_t* dims, const float* origin, float h, const 
   M::profile.p = profile.data();
   set_shape(M::shape, shape);
   set_rig(M::rig);
+  set_car_textures(M::carSdf, M::carParts);
   M::cam.pos = v3(cam); M::cam.tanHalf = cam[3];
   M::cam.fwd = v3(cam + 4); M::cam.aspect = cam[7];
   M::cam.right = v3(cam + 8); M::cam.time = cam[11];
@@ -357,11 +388,29 @@ void wtr_render_scene(const uint32_t* dims, const float* origin, float h, const 
   });
 }
 
+// The W17 model (engine.ts:410-421 setCarModel and the rig uniform of setShape):
+// sdf 368 x 84 x 67 binary16 (x fastest), parts pd[0] x pd[1] x pd[2] binary16,
+// rig the 87 vec4 of the Rig uniform (car-model.ts:60-69).  sdf == NULL clears it.
+void wtr_set_car(const uint16_t* sdf, const uint16_t* parts, const uint32_t* pd, const float* rig) {
+  if (!sdf) {
+    g_car = CarModel{};
+    return;
+  }
+  g_car.sdf.assign(sdf, sdf + 368 * 84 * 67);
+  for (int i = 0; i < 3; i++) g_car.pdims[i] = (int)pd[i];
+  g_car.parts.assign(parts, parts + (size_t)pd[0] * pd[1] * pd[2]);
+  memcpy(g_car.rig, rig, sizeof(g_car.rig));
+  g_car.set = true;
+}
+
 // sceneSdf (the RENDER module's copy of the SDF chunk) at n points: out[2k], out[2k+1].
 void wtr_scene_sdf(const uint32_t* shape, const float* pts, uint32_t n, float* out) {
   namespace M = m_render;
   set_shape(M::shape, shape);
   set_rig(M::rig);
+  set_car_textures(M::carSdf, M::carParts);
+  static std::vector<float> profile(256 * 128, 10.0f);
+  M::profile.p = profile.data();
   for (uint32_t k = 0; k < n; k++) {
     const rt::vec2f r = M::sceneSdf(rt::vec3f(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]));
     out[2 * k] = r.x;

@@ -11,6 +11,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <vector>
+
 #include <cuda_runtime.h>
 
 static inline float __fsqrt_rn(float x) { return sqrtf(x); }
@@ -33,7 +35,29 @@ static inline T __ldg(const T* p) { return *p; }
 
 using namespace wt;
 
+namespace {
+// the W17 model of wthm_set_car (host copies the shading code reads)
+std::vector<uint16_t> g_body, g_parts;
+std::vector<float4> g_rig;
+CarView g_car;
+}  // namespace
+
 extern "C" {
+
+// The W17 model: body 368 x 84 x 67 and parts pd[0] x pd[1] x pd[2] binary16, rig
+// the 87 vec4 of the Rig uniform.  body == NULL clears it.
+void wthm_set_car(const uint16_t* body, const uint16_t* parts, const uint32_t* pd, const float* rig) {
+  g_car = CarView{};
+  if (!body) return;
+  g_body.assign(body, body + (size_t)368 * 84 * 67);
+  g_parts.assign(parts, parts + (size_t)pd[0] * pd[1] * pd[2]);
+  g_rig.resize(87);
+  memcpy(g_rig.data(), rig, 87 * sizeof(float4));
+  g_car.body = g_body.data();
+  g_car.parts = g_parts.data();
+  for (int i = 0; i < 3; i++) g_car.pdims[i] = pd[i];
+  g_car.rig = g_rig.data();
+}
 
 // RENDER fs_main over rows [y0, y1) of a w x h target: out[(y*w + x)*4 + k] =
 // colour, hit distance (rows outside the range untouched).  shape: wt_shape;
@@ -74,7 +98,8 @@ void wthm_render(const void* shape, const void* cam_p, const void* look_p, const
   a.fill_a = f3n(0.6f, 0.35f, -0.7f);
   a.fill_b = f3n(0.6f, 0.35f, 0.7f);
   a.w = w; a.h = hgt;
-  const Scene S = make_scene(a.shape);
+  a.car = g_car;
+  const Scene S = make_scene(a.shape, g_car);
   for (uint32_t y = y0; y < y1 && y < hgt; y++)
     for (uint32_t x = 0; x < w; x++) {
       const float4 c = render_pixel(S, a, x, y);
@@ -87,7 +112,7 @@ void wthm_render(const void* shape, const void* cam_p, const void* look_p, const
 void wthm_scene_sdf(const void* shape, const float* pts, uint32_t n, float* out) {
   wt_shape sh;
   memcpy(&sh, shape, sizeof sh);
-  const Scene S = make_scene(sh);
+  const Scene S = make_scene(sh, g_car);
   for (uint32_t k = 0; k < n; k++) {
     const V2 r = scene_sdf(S, v3(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]));
     out[2 * k] = r.x;

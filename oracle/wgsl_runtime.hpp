@@ -187,11 +187,56 @@ template <class T> struct storage {
   T* p = nullptr;
   T& operator[](int64_t i) const { return p[i]; }
 };
-struct texture3d { int dummy = 0; };
+// A 3-D r16float texture (the baked W17 model: body SDF and parts atlas),
+// w x h x d binary16 texels, x fastest; no data = the engine's unwritten
+// texture, which samples as 0.
+struct texture3d {
+  int w = 1, h = 1, d = 1;
+  const uint16_t* p = nullptr;
+};
 struct sampler { int dummy = 0; };
-// Textures only feed the baked-mesh (W17) scene, which this model does not evaluate.
-static inline vec4f textureSampleLevel(const texture3d&, const sampler&, vec3f, f32) { return vec4f(0.0f); }
-static inline vec3u textureDimensions(const texture3d&) { return vec3u(1u, 1u, 1u); }
+static inline f32 half_bits_to_f32(uint16_t b) {
+  const uint32_t sign = (uint32_t)(b >> 15) << 31, e = (b >> 10) & 0x1fu, m = b & 0x3ffu;
+  uint32_t u;
+  if (e == 0x1fu) u = sign | 0x7f800000u | (m << 13);
+  else if (e != 0) u = sign | ((e + 112u) << 23) | (m << 13);
+  else if (m == 0) u = sign;
+  else {  // subnormal: m * 2^-24, exact in binary32
+    f32 v = (f32)m * 5.9604644775390625e-8f;
+    memcpy(&u, &v, 4);
+    u |= sign;
+  }
+  f32 r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+// textureSampleLevel with a linear, clamp-to-edge sampler at level 0 (the
+// engine's carSamp, engine.ts:270), written out with f32 weights: texel
+// coordinate c = uvw * size - 0.5, i = floor(c), t = c - i, indices clamped to
+// the texture, blended along x, then y, then z with mix(a, b, t) = a (1 - t) + b t.
+// (A GPU's filter hardware uses reduced-precision weights; WebGPU leaves that
+// precision to the implementation.)
+static inline f32 texel3(const texture3d& t, int x, int y, int z) {
+  x = x < 0 ? 0 : (x >= t.w ? t.w - 1 : x);
+  y = y < 0 ? 0 : (y >= t.h ? t.h - 1 : y);
+  z = z < 0 ? 0 : (z >= t.d ? t.d - 1 : z);
+  return half_bits_to_f32(t.p[((size_t)z * (size_t)t.h + (size_t)y) * (size_t)t.w + (size_t)x]);
+}
+static inline int floor_index(f32 f, int n) { return (int)(f < -1.0f ? -1.0f : (f > (f32)n ? (f32)n : f)); }
+static inline vec4f textureSampleLevel(const texture3d& t, const sampler&, vec3f uvw, f32) {
+  if (!t.p) return vec4f(0.0f);
+  const f32 cx = uvw.x * (f32)t.w - 0.5f, cy = uvw.y * (f32)t.h - 0.5f, cz = uvw.z * (f32)t.d - 0.5f;
+  const f32 fx = __builtin_floorf(cx), fy = __builtin_floorf(cy), fz = __builtin_floorf(cz);
+  const f32 tx = cx - fx, ty = cy - fy, tz = cz - fz;
+  const int i = floor_index(fx, t.w), j = floor_index(fy, t.h), k = floor_index(fz, t.d);
+  const f32 c00 = texel3(t, i, j, k) * (1.0f - tx) + texel3(t, i + 1, j, k) * tx;
+  const f32 c10 = texel3(t, i, j + 1, k) * (1.0f - tx) + texel3(t, i + 1, j + 1, k) * tx;
+  const f32 c01 = texel3(t, i, j, k + 1) * (1.0f - tx) + texel3(t, i + 1, j, k + 1) * tx;
+  const f32 c11 = texel3(t, i, j + 1, k + 1) * (1.0f - tx) + texel3(t, i + 1, j + 1, k + 1) * tx;
+  const f32 c0 = c00 * (1.0f - ty) + c10 * ty, c1 = c01 * (1.0f - ty) + c11 * ty;
+  return vec4f(c0 * (1.0f - tz) + c1 * tz, 0.0f, 0.0f, 1.0f);
+}
+static inline vec3u textureDimensions(const texture3d& t) { return vec3u((u32)t.w, (u32)t.h, (u32)t.d); }
 // A 2-D render target read by textureLoad: w x h texels of RGBA f32 (already
 // rounded to the target format by whoever wrote it).
 struct texture2d {

@@ -10,7 +10,7 @@ after five passes and its streamlines).  The fixed-function stages (viewport,
 rasterization, blending) are the oracle's restatement of the WebGPU pipeline
 (oracle/ref_driver.cpp).
 
-Nine sequences of frames at 128x72 cover the scene pass's branches:
+Ten sequences of frames at 128x72 cover the scene pass's branches:
   hero      livery, ground reflection and belt, streamline glow; then a second
             frame from a slightly moved camera, which reprojects the history
   surface   pressure colour on the body surface (surfMode 1, palette 1)
@@ -20,6 +20,8 @@ Nine sequences of frames at 128x72 cover the scene pass's branches:
   cube, sphere, wing, empty
             the other analytic scenes: carbon and paint bodies, vorticity colour
             on a sphere's surface, a pressure slice past the wing, the bare tunnel
+  w17       the baked W17 scene with the synthetic stand-in model (rig-rotated
+            wing parts, squeezed sidepods), pressure colour on its surface
 Stored per frame: the scene, resolved history, glow and bloom B targets
 (binary16) and the presented RGBA8 output.
 
@@ -41,6 +43,7 @@ sys.path.insert(0, HERE)
 import make_consumers as mc  # noqa: E402
 from windtunnel import render as R  # noqa: E402
 from windtunnel.engine import ShapeKind, ShapeParams  # noqa: E402
+from windtunnel.car_model import synthetic_w17  # noqa: E402
 from windtunnel.workloads import config_f1_shape  # noqa: E402
 
 OUT = os.path.join(HERE, "render.npz")
@@ -86,6 +89,12 @@ def sequences(z):
         ("empty", [dict(cam=R.orbit_camera((2.0, 0.5, 0.0), 2.0, 0.4, 7.0, asp),
                         look=R.make_look(empty, palette=0, slice_axis=2, slice_pos=0.5), shape=empty)]),
     ]
+    # the baked W17 scene (kind 5) with the synthetic stand-in model, open cooling
+    w17 = ShapeParams(kind=ShapeKind.W17, rideH=0.10, rearRideH=0.15, frontFlapDeg=5.0, rearShape=1, sidepods=1,
+                      cooling=2)
+    seqs.append(("w17", [dict(cam=R.orbit_camera((2.6, 0.45, 0.0), 2.4, 0.3, 6.2, asp),
+                              look=R.make_look(w17, palette=1, surface_field=True), shape=w17,
+                              car=synthetic_w17(w17))]))
     return shape, seqs
 
 
@@ -113,6 +122,7 @@ def main():
         hist = [np.zeros((H, W, 4), np.float32), np.zeros((H, W, 4), np.float32)]
         for k, f in enumerate(frames):
             u = frame_uniforms(st, f)
+            pyoracle.ref_set_car(f.get("car"))
             scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, z["fields"], z["temps"], frame_shape(shape, f),
                                               u.cam, f["look"], view, W, H)
             hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)

@@ -37,6 +37,8 @@ def test_render_frames_bitexact(setup):
     mc, mr, z, e, seqs, shape, c = setup
     view = mc.view()
     for name, frames in seqs:
+        if "car" in frames[0]:
+            e.set_car_model(frames[0]["car"])
         e.set_shape_raw(mr.frame_shape(shape, frames[0]))  # the renderer draws the context's shape
         e.write_state(fields=c["fields"], temps=c["temps"])
         r = R.Renderer(e, mr.W, mr.H)

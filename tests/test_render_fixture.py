@@ -28,7 +28,7 @@ def test_fixture_is_consistent():
     z = fixture()
     keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
     assert keys == ["cube_0", "empty_0", "hero_0", "hero_1", "slice-x_0", "slice-y_0", "slice-z_0", "sphere_0",
-                    "surface_0", "wing_0"]
+                    "surface_0", "w17_0", "wing_0"]
     for k in keys:
         sc, out = z[k + "_scene"].astype(np.float32), z[k + "_out"]
         assert sc.shape == (mr.H, mr.W, 4) and out.shape == (mr.H, mr.W, 4) and out.dtype == np.uint8
@@ -57,6 +57,7 @@ def test_reference_reproduces_fixture():
         hist = [np.zeros((mr.H, mr.W, 4), np.float32) for _ in range(2)]
         for k, f in enumerate(frames):
             u = mr.frame_uniforms(st, f)
+            pyoracle.ref_set_car(f.get("car"))
             scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, c["fields"], c["temps"],
                                               mr.frame_shape(shape, f), u.cam, f["look"], mc.view(), mr.W, mr.H)
             hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)

@@ -82,6 +82,7 @@ def test_device_render_pixel_matches_fixture(hm):
         for k, f in enumerate(frames):
             u = mr.frame_uniforms(st, f)
             from oracle import pyoracle
+            pyoracle.shade_model_set_car(f.get("car"))
             out = pyoracle.shade_model_render(mr.frame_shape(shape, f), u.cam, f["look"], view, dims, org, mc.H,
                                               c["fields"], c["temps"], mr.W, mr.H, threads=4)
             ref = z[f"{name}_{k}_scene"]
