@@ -63,3 +63,11 @@ def shade_host_model():
     headers are missing."""
     from oracle import pyoracle
     return pyoracle.shade_model_lib()
+
+
+def same_half(a, b):
+    """binary16 arrays equal bit for bit, except that any NaN equals any NaN (the
+    payload a NaN gets when rounded to binary16 is the implementation's)."""
+    a = np.ascontiguousarray(a, np.float16)
+    b = np.ascontiguousarray(b, np.float16)
+    return (a.view(np.uint16) == b.view(np.uint16)) | (np.isnan(a) & np.isnan(b))

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
+from helpers import same_half
 
 pytestmark = pytest.mark.gpu
 
@@ -59,7 +60,7 @@ def check_sequence(r, name, frames, z, view):
                "glow": r.read(R.TARGET_GLOW), "bloom": r.read(R.TARGET_BLOOM_B)}
         for t, v in got.items():
             ref = z[f"{key}_{t}"]
-            bad = np.argwhere(np.any(v.view(np.uint16) != ref.view(np.uint16), axis=-1))
+            bad = np.argwhere(np.any(~same_half(v, ref), axis=-1))
             assert len(bad) == 0, f"{key} {t}: {len(bad)} texels differ, first {bad[:4].tolist()}"
         assert np.array_equal(r.read(R.TARGET_OUTPUT), z[key + "_out"]), key
 

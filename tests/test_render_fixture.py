@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
+from helpers import same_half
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 sys.path.insert(0, GOLDEN)
@@ -33,7 +34,10 @@ def test_fixture_is_consistent():
         sc, out = z[k + "_scene"].astype(np.float32), z[k + "_out"]
         assert sc.shape == (mr.H, mr.W, 4) and out.shape == (mr.H, mr.W, 4) and out.dtype == np.uint8
         assert z[k + "_bloom"].shape == (mr.H // 2, mr.W // 2, 4)
-        assert np.isfinite(sc).all() and (sc[..., 3] > 0).all() and (sc[..., 3] <= 6e4).all()
+        # colours are finite except where the reference's normal estimate degenerates (four equal
+        # distance taps on a quantized texture give normalize(0): NaN, as in the shader itself)
+        assert np.isfinite(sc[..., 3]).all() and (sc[..., 3] > 0).all() and (sc[..., 3] <= 6e4).all()
+        assert (~np.isfinite(sc[..., :3])).any(axis=-1).mean() < 1e-3
         assert (out[..., 3] == 255).all()
         assert (z[k + "_glow"].astype(np.float32) >= 0).all()
     # the car is in view, the glow draws hit pixels, history reprojection changed the second frame
@@ -67,7 +71,7 @@ def test_reference_reproduces_fixture():
             out = pyoracle.ref_present(hist[u.cur], glow, bb, u.post)
             key = f"{name}_{k}"
             for t, v in zip(TARGETS, (scene, hist[u.cur], glow, bb)):
-                assert np.array_equal(v.astype(np.float16).view(np.uint16), z[f"{key}_{t}"].view(np.uint16)), (key, t)
+                assert same_half(v, z[f"{key}_{t}"]).all(), (key, t)
             assert np.array_equal(out, z[key + "_out"]), key
 
 

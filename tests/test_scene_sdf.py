@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
-from helpers import golden_shapes, shade_host_model
+from helpers import golden_shapes, same_half, shade_host_model
 
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 
@@ -86,5 +86,5 @@ def test_device_render_pixel_matches_fixture(hm):
             out = pyoracle.shade_model_render(mr.frame_shape(shape, f), u.cam, f["look"], view, dims, org, mc.H,
                                               c["fields"], c["temps"], mr.W, mr.H, threads=4)
             ref = z[f"{name}_{k}_scene"]
-            bad = np.argwhere(np.any(out.astype(np.float16).view(np.uint16) != ref.view(np.uint16), axis=-1))
+            bad = np.argwhere(np.any(~same_half(out, ref), axis=-1))
             assert len(bad) == 0, f"{name}_{k}: {len(bad)} pixels differ, first {bad[:4].tolist()}"
