@@ -150,8 +150,11 @@ def test_errors_are_reported(wt_lib):
     with pytest.raises(WindTunnelError, match="heat_passes"):
         e.step(2, 1)
     s = Shape()
-    s.kind = 5
+    s.kind = 4  # the custom 2-D profile scene
     with pytest.raises(WindTunnelError, match="not built"):
+        e.set_shape_raw(s)
+    s.kind = 5  # the W17 scene without its model
+    with pytest.raises(WindTunnelError, match="car model"):
         e.set_shape_raw(s)
     with pytest.raises(WindTunnelError):
         AeroEngine(dims=(4, 1, 1), h=0.1)
