@@ -106,10 +106,16 @@ __device__ V3 seed_of(const StreamArgs& st, uint32_t line) {
   return v3(st.smin[0], wmix(st.smin[1], st.smax[1], fy), wmix(st.smin[2], st.smax[2], fz));
 }
 
-// Streamline pass cs_main (render-wgsl.ts:551-575): one thread per line.
-__global__ void streamlines_kernel(FieldGrid g, StreamArgs st, ViewArgs view, float4* __restrict__ pts) {
-  const uint32_t line = blockIdx.x * blockDim.x + threadIdx.x;
-  if (line >= st.lines) return;
+// Streamline pass cs_main (render-wgsl.ts:551-575): one line per block of one
+// warp, lane 0 only.  A line is a chain of dependent RK2 steps, two field samples
+// each; lines packed 32 to a warp would gather from 32 places per load (32 L1
+// lookups per instruction) and sit on a couple of SMs.  One line per warp spreads
+// the (at most a few hundred) lines over the SMs and leaves each gather a single
+// lookup, so each step costs about one L1 round trip per sample.
+__global__ void __launch_bounds__(32) streamlines_kernel(FieldGrid g, StreamArgs st, ViewArgs view,
+                                                        float4* __restrict__ pts) {
+  const uint32_t line = blockIdx.x;
+  if (line >= st.lines || threadIdx.x != 0) return;
   const uint32_t base = line * st.steps;
   V3 p = seed_of(st, line);
   bool alive = true;
@@ -157,7 +163,7 @@ cudaError_t launch_particles(const FieldGrid& g, const PSimArgs& ps, const ViewA
 cudaError_t launch_streamlines(const FieldGrid& g, const StreamArgs& st, const ViewArgs& v, float4* pts,
                                cudaStream_t s) {
   if (st.lines == 0) return cudaSuccess;
-  streamlines_kernel<<<(st.lines + 63) / 64, 64, 0, s>>>(g, st, v, pts);
+  streamlines_kernel<<<st.lines, 32, 0, s>>>(g, st, v, pts);
   return cudaGetLastError();
 }
 
