@@ -1,0 +1,59 @@
+"""Known answers of the lattice physics on the GPU through the C ABI (the oracle
+twin is tests/test_known_answers.py): uniform flow is a fixed point, the
+single-cell momentum exchange is 2 rho u, and the drag coefficient of the cube
+configuration (128x64x64, 22-cell cube on the belt, 1000 steps, mean over steps
+500-999) lies in a band around the reference README's Cd of about 1.04."""
+import numpy as np
+import pytest
+
+from test_known_answers import DIMS, U_IN, single_cell, uniform_equilibrium
+
+pytestmark = pytest.mark.gpu
+
+
+def test_uniform_flow_is_a_fixed_point_gpu(wt_lib):
+    from windtunnel import AeroEngine
+    from windtunnel.engine import make_sim
+    e = AeroEngine(dims=DIMS, origin=(0, 0, 0), h=0.1, sim=make_sim(u_in=U_IN, tau0=0.52, smag=0.15))
+    e.reset()
+    f0 = e.read_populations().astype(np.float64)
+    np.testing.assert_allclose(f0, uniform_equilibrium(int(np.prod(DIMS)), U_IN), atol=3e-8)
+    e.step(240, 0)
+    early = np.abs(e.read_populations() - f0).max()
+    e.step(960, 0)
+    late = np.abs(e.read_populations() - f0).max()
+    assert early < 2e-6 and late < 2e-6 and late <= 1.5 * early
+    d = e.debug_read()
+    np.testing.assert_allclose(d["fields"][:, 0], U_IN, atol=2e-6)
+    np.testing.assert_allclose(d["fields"][:, 3], 1.0, atol=2e-6)
+    e.close()
+
+
+def test_single_cell_momentum_exchange_gpu(wt_lib):
+    from windtunnel import AeroEngine
+    from windtunnel.engine import make_sim
+    e = AeroEngine(dims=DIMS, origin=(0, 0, 0), h=0.1, sim=make_sim(u_in=U_IN, tau0=0.52, smag=0.15))
+    e.set_solid(*single_cell(DIMS, 20, 6, 7))
+    e.reset()
+    e.step(2, 0)
+    first = e.force_history(2)[0]       # the first step's per-component sums
+    assert abs(first[0] - 2 * U_IN) < 1e-6 and abs(first[1]) < 1e-7 and abs(first[2]) < 1e-7
+    e.close()
+
+
+def test_cube_drag_coefficient_band(wt_lib):
+    from windtunnel import AeroEngine, cube_config
+    from windtunnel.workloads import drag_coefficient, half_area_cells
+    dims, origin, h, sim, shape = cube_config()
+    e = AeroEngine(dims=dims, origin=origin, h=h, sim=sim)
+    e.set_shape_raw(shape)
+    e.reset()
+    e.step(500, 0)
+    e.read_forces_raw(reset=True)
+    e.step(500, 0)
+    fr = e.read_forces_raw(reset=True)
+    area = half_area_cells(e.debug_read()["solid"], dims)
+    cd = drag_coefficient(fr.sum[0] / fr.steps, sim.u_in, area)
+    print(f"\ncube Cd over steps 500-999: {cd:.4f} (area {area} cells)")
+    assert 0.6 < cd < 1.6
+    e.close()

@@ -1,0 +1,57 @@
+"""Known answers of the lattice physics, independent of any reference run, on
+the oracle (the GPU twin is tests/test_gpu_known_answers.py):
+
+* uniform flow through the empty tunnel (velocity inlet, moving belt at the
+  inlet speed, far field, symmetry plane, outlet) is a fixed point: an
+  equilibrium start stays there to float round-off;
+* momentum exchange on a single solid cell in uniform flow after one step is
+  the analytic 2 rho u (wgsl.ts:221-223: every one of the 18 fluid neighbours
+  bounces feq_opp(i) back and records -2 (v - w_i) c_i, which sums to
+  2 sum_j (feq_j - w_j) c_j = 2 rho u), with no lift or side force.
+"""
+import numpy as np
+
+U_IN = 0.08
+DIMS = (48, 20, 16)
+
+
+def uniform_equilibrium(n, u):
+    cx = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0], np.float64)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    feq = w * (1 + 3 * cx * u + 4.5 * (cx * u) ** 2 - 1.5 * u * u)
+    return np.repeat(feq, n)
+
+
+def single_cell(dims, x, y, z):
+    n = int(np.prod(dims))
+    solid = np.zeros(n, np.uint32)
+    solid[x + dims[0] * (y + dims[1] * z)] = 1
+    return solid, np.zeros(n, np.float32)
+
+
+def test_uniform_flow_is_a_fixed_point(oracle_mod):
+    from windtunnel.engine import make_sim
+    o = oracle_mod.Oracle(DIMS, (0, 0, 0), 0.1, make_sim(u_in=U_IN, tau0=0.52, smag=0.15))
+    o.reset()
+    f0 = o.read()["f"].astype(np.float64)
+    np.testing.assert_allclose(f0, uniform_equilibrium(int(np.prod(DIMS)), U_IN), atol=3e-8)
+    o.steps(240)
+    early = np.abs(o.read()["f"] - f0).max()
+    o.steps(960)
+    d = o.read()
+    late = np.abs(d["f"] - f0).max()
+    # float round-off of the moments and feq (a few ulp of 1/3), bounded: no drift
+    assert early < 2e-6 and late < 2e-6 and late <= 1.5 * early
+    np.testing.assert_allclose(d["fields"][:, 0], U_IN, atol=2e-6)
+    np.testing.assert_allclose(d["fields"][:, 1:3], 0.0, atol=2e-6)
+    np.testing.assert_allclose(d["fields"][:, 3], 1.0, atol=2e-6)
+
+
+def test_single_cell_momentum_exchange(oracle_mod):
+    from windtunnel.engine import make_sim
+    o = oracle_mod.Oracle(DIMS, (0, 0, 0), 0.1, make_sim(u_in=U_IN, tau0=0.52, smag=0.15))
+    o.set_solid(*single_cell(DIMS, 20, 6, 7))
+    o.reset()
+    o.steps(1)
+    fx, fy, fz = o.read(reset_forces=True)["forces64"][:3]
+    assert abs(fx - 2 * U_IN) < 1e-6 and abs(fy) < 1e-7 and abs(fz) < 1e-7
