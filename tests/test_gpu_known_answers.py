@@ -1,8 +1,8 @@
 """Known answers of the lattice physics on the GPU through the C ABI (the oracle
 twin is tests/test_known_answers.py): uniform flow is a fixed point, the
-single-cell momentum exchange is 2 rho u, and the drag coefficient of the cube
-configuration (128x64x64, 22-cell cube on the belt, 1000 steps, mean over steps
-500-999) lies in a band around the reference README's Cd of about 1.04."""
+single-cell momentum exchange is 2 rho u, and the drag coefficient of the
+reference's cube scene in the medium tunnel, averaged over steps 500-999, is the
+README's Cd of about 1.04."""
 import numpy as np
 import pytest
 
@@ -42,18 +42,23 @@ def test_single_cell_momentum_exchange_gpu(wt_lib):
 
 
 def test_cube_drag_coefficient_band(wt_lib):
-    from windtunnel import AeroEngine, cube_config
+    """The reference's own cube scene (wgsl.ts:105: a 1 m rounded cube at (2.6, 1, 0))
+    in the medium tunnel (232x68x52) from the engine's default flow: the mean
+    drag coefficient over steps 500-999 is the README's "Cd about 1.04" to a
+    few percent (measured 1.067; the impulsively started flow keeps developing
+    afterwards, to about 1.37 by step 12000)."""
+    from windtunnel import AeroEngine
+    from windtunnel.engine import ShapeKind, ShapeParams
     from windtunnel.workloads import drag_coefficient, half_area_cells
-    dims, origin, h, sim, shape = cube_config()
-    e = AeroEngine(dims=dims, origin=origin, h=h, sim=sim)
-    e.set_shape_raw(shape)
+    e = AeroEngine("medium")
+    e.set_shape(ShapeParams(kind=ShapeKind.Cube))
     e.reset()
     e.step(500, 0)
     e.read_forces_raw(reset=True)
     e.step(500, 0)
     fr = e.read_forces_raw(reset=True)
-    area = half_area_cells(e.debug_read()["solid"], dims)
-    cd = drag_coefficient(fr.sum[0] / fr.steps, sim.u_in, area)
+    area = half_area_cells(e.debug_read()["solid"], e.dims)
+    cd = drag_coefficient(fr.sum[0] / fr.steps, e.sim.u_in, area)
     print(f"\ncube Cd over steps 500-999: {cd:.4f} (area {area} cells)")
-    assert 0.6 < cd < 1.6
+    assert 0.95 < cd < 1.15
     e.close()
