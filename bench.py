@@ -390,7 +390,7 @@ def main():
     ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "surrogate", "render"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--cpu-frames", type=int, default=4)
+    ap.add_argument("--cpu-frames", type=int, default=64, help="CPU-baseline frames (stops at 20 s)")
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=64, help="LBM steps per kernel-timing launch batch")
