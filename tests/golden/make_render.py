@@ -10,7 +10,7 @@ after five passes and its streamlines).  The fixed-function stages (viewport,
 rasterization, blending) are the oracle's restatement of the WebGPU pipeline
 (oracle/ref_driver.cpp).
 
-Ten sequences of frames at 128x72 cover the scene pass's branches:
+Eleven sequences of frames (128x72 unless noted) cover the scene pass's branches:
   hero      livery, ground reflection and belt, streamline glow; then a second
             frame from a slightly moved camera, which reprojects the history
   surface   pressure colour on the body surface (surfMode 1, palette 1)
@@ -22,6 +22,8 @@ Ten sequences of frames at 128x72 cover the scene pass's branches:
             on a sphere's surface, a pressure slice past the wing, the bare tunnel
   w17       the baked W17 scene with the synthetic stand-in model (rig-rotated
             wing parts, squeezed sidepods), pressure colour on its surface
+  tiny      a ragged 17x9 target (8x4 bloom) with particle and streamline glow,
+            two frames
 Stored per frame: the scene, resolved history, glow and bloom B targets
 (binary16) and the presented RGBA8 output.
 
@@ -95,6 +97,10 @@ def sequences(z):
     seqs.append(("w17", [dict(cam=R.orbit_camera((2.6, 0.45, 0.0), 2.4, 0.3, 6.2, asp),
                               look=R.make_look(w17, palette=1, surface_field=True), shape=w17,
                               car=synthetic_w17(w17))]))
+    # a ragged target: 17x9 (bloom targets 8x4), particle and streamline glow, two frames
+    tiny = dict(cam=R.orbit_camera((2.75, 0.42, 0.0), 2.3, 0.3, 7.6, 17 / 9), look=R.make_look(p, palette=0),
+                parts=parts, lines=z["lines_rake"], color_mode=0, flow_time=0.3, size=(17, 9))
+    seqs.append(("tiny", [tiny, dict(tiny, cam=R.orbit_camera((2.75, 0.42, 0.0), 2.35, 0.31, 7.4, 17 / 9))]))
     return shape, seqs
 
 
@@ -104,8 +110,12 @@ def frame_shape(default, f):
     return pack_shape(f["shape"]) if "shape" in f else default
 
 
+def frame_size(f):
+    return f.get("size", (W, H))
+
+
 def frame_uniforms(state, f):
-    return state.next(f["cam"], (W, H), parts=f.get("parts"), color_mode=f.get("color_mode", 0),
+    return state.next(f["cam"], frame_size(f), parts=f.get("parts"), color_mode=f.get("color_mode", 0),
                       smoke=f.get("smoke", True), lines=f.get("lines"), flow_time=f.get("flow_time", 0.0),
                       vortices=f.get("vortices", False))
 
@@ -115,16 +125,17 @@ def main():
     z = np.load(os.path.join(HERE, "consumers.npz"))
     shape, seqs = sequences(z)
     view = mc.view()
-    hw, hh = W // 2, H // 2
     out = {}
     for name, frames in seqs:
         st = R.FrameState()
-        hist = [np.zeros((H, W, 4), np.float32), np.zeros((H, W, 4), np.float32)]
+        w, h = frame_size(frames[0])
+        hw, hh = max(1, w // 2), max(1, h // 2)
+        hist = [np.zeros((h, w, 4), np.float32), np.zeros((h, w, 4), np.float32)]
         for k, f in enumerate(frames):
             u = frame_uniforms(st, f)
             pyoracle.ref_set_car(f.get("car"))
             scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, z["fields"], z["temps"], frame_shape(shape, f),
-                                              u.cam, f["look"], view, W, H)
+                                              u.cam, f["look"], view, w, h)
             hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)
             glow = pyoracle.ref_glow(scene, f.get("parts"), u.pdraw, f.get("lines"), u.sdraw)
             ba = pyoracle.ref_blur(glow, (1.0, 0.0), 3.0, 1.0, hw, hh)

@@ -42,7 +42,7 @@ def test_render_frames_bitexact(setup):
             e.set_car_model(frames[0]["car"])
         e.set_shape_raw(mr.frame_shape(shape, frames[0]))  # the renderer draws the context's shape
         e.write_state(fields=c["fields"], temps=c["temps"])
-        r = R.Renderer(e, mr.W, mr.H)
+        r = R.Renderer(e, *mr.frame_size(frames[0]))
         try:
             check_sequence(r, name, frames, z, view)
         finally:

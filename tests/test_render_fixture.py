@@ -29,11 +29,12 @@ def test_fixture_is_consistent():
     z = fixture()
     keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
     assert keys == ["cube_0", "empty_0", "hero_0", "hero_1", "slice-x_0", "slice-y_0", "slice-z_0", "sphere_0",
-                    "surface_0", "w17_0", "wing_0"]
+                    "surface_0", "tiny_0", "tiny_1", "w17_0", "wing_0"]
     for k in keys:
         sc, out = z[k + "_scene"].astype(np.float32), z[k + "_out"]
-        assert sc.shape == (mr.H, mr.W, 4) and out.shape == (mr.H, mr.W, 4) and out.dtype == np.uint8
-        assert z[k + "_bloom"].shape == (mr.H // 2, mr.W // 2, 4)
+        w, h = (17, 9) if k.startswith("tiny") else (mr.W, mr.H)
+        assert sc.shape == (h, w, 4) and out.shape == (h, w, 4) and out.dtype == np.uint8
+        assert z[k + "_bloom"].shape == (h // 2, w // 2, 4)
         # colours are finite except where the reference's normal estimate degenerates (four equal
         # distance taps on a quantized texture give normalize(0): NaN, as in the shader itself)
         assert np.isfinite(sc[..., 3]).all() and (sc[..., 3] > 0).all() and (sc[..., 3] <= 6e4).all()
@@ -58,16 +59,17 @@ def test_reference_reproduces_fixture():
     shape, seqs = mr.sequences(c)
     for name, frames in seqs:
         st = R.FrameState()
-        hist = [np.zeros((mr.H, mr.W, 4), np.float32) for _ in range(2)]
+        w, h = mr.frame_size(frames[0])
+        hw, hh = max(1, w // 2), max(1, h // 2)
+        hist = [np.zeros((h, w, 4), np.float32) for _ in range(2)]
         for k, f in enumerate(frames):
             u = mr.frame_uniforms(st, f)
             pyoracle.ref_set_car(f.get("car"))
             scene = pyoracle.ref_render_scene(mc.DIMS, mc.ORIGIN, mc.H, c["fields"], c["temps"],
-                                              mr.frame_shape(shape, f), u.cam, f["look"], mc.view(), mr.W, mr.H)
+                                              mr.frame_shape(shape, f), u.cam, f["look"], mc.view(), w, h)
             hist[u.cur] = pyoracle.ref_taa(scene, hist[1 - u.cur], u.taa)
             glow = pyoracle.ref_glow(scene, f.get("parts"), u.pdraw, f.get("lines"), u.sdraw)
-            bb = pyoracle.ref_blur(pyoracle.ref_blur(glow, (1.0, 0.0), 3.0, 1.0, mr.W // 2, mr.H // 2), (0.0, 1.0),
-                                   1.5, 1.0, mr.W // 2, mr.H // 2)
+            bb = pyoracle.ref_blur(pyoracle.ref_blur(glow, (1.0, 0.0), 3.0, 1.0, hw, hh), (0.0, 1.0), 1.5, 1.0, hw, hh)
             out = pyoracle.ref_present(hist[u.cur], glow, bb, u.post)
             key = f"{name}_{k}"
             for t, v in zip(TARGETS, (scene, hist[u.cur], glow, bb)):

@@ -83,8 +83,9 @@ def test_device_render_pixel_matches_fixture(hm):
             u = mr.frame_uniforms(st, f)
             from oracle import pyoracle
             pyoracle.shade_model_set_car(f.get("car"))
+            w, h = mr.frame_size(f)
             out = pyoracle.shade_model_render(mr.frame_shape(shape, f), u.cam, f["look"], view, dims, org, mc.H,
-                                              c["fields"], c["temps"], mr.W, mr.H, threads=4)
+                                              c["fields"], c["temps"], w, h, threads=4)
             ref = z[f"{name}_{k}_scene"]
             bad = np.argwhere(np.any(~same_half(out, ref), axis=-1))
             assert len(bad) == 0, f"{name}_{k}: {len(bad)} pixels differ, first {bad[:4].tolist()}"
