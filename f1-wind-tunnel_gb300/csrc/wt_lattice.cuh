@@ -68,6 +68,8 @@ __device__ __forceinline__ float div_rcp(float a, float b, float r) {
 struct StoreF32 {
   typedef float T;
   static constexpr uint32_t id = 0;
+  // step-kernel blocks of 256 per SM: 48 registers; the extra warps hide HBM latency
+  static constexpr int min_blocks = 5;
   __device__ __forceinline__ static float ld(const T* p, float) { return __ldg(p); }
   __device__ __forceinline__ static float ld_smem(const T* p, float) { return *p; }
   __device__ __forceinline__ static void st(T* p, float v, float) { *p = v; }
@@ -82,6 +84,8 @@ constexpr float F16_SCALE = 16384.0f, F16_INV = 1.0f / 16384.0f;
 struct StoreF16 {
   typedef __half T;
   static constexpr uint32_t id = 1;
+  // step-kernel blocks of 256 per SM: 64 registers (the collision, not HBM, bounds it)
+  static constexpr int min_blocks = 4;
   __device__ __forceinline__ static float ld(const T* p, float w) { return __fmaf_rn(__half2float(__ldg(p)), F16_INV, w); }
   __device__ __forceinline__ static float ld_smem(const T* p, float w) { return __fmaf_rn(__half2float(*p), F16_INV, w); }
   __device__ __forceinline__ static void st(T* p, float v, float w) {
@@ -91,6 +95,8 @@ struct StoreF16 {
 struct StoreBF16 {
   typedef __nv_bfloat16 T;
   static constexpr uint32_t id = 2;
+  // step-kernel blocks of 256 per SM: 64 registers (the collision, not HBM, bounds it)
+  static constexpr int min_blocks = 4;
   __device__ __forceinline__ static float ld(const T* p, float w) { return w + __bfloat162float(__ldg(p)); }
   __device__ __forceinline__ static float ld_smem(const T* p, float w) { return w + __bfloat162float(*p); }
   __device__ __forceinline__ static void st(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }

@@ -569,7 +569,7 @@ cudaError_t launch_chained(K kernel, dim3 grid, dim3 block, cudaStream_t s, Args
 }
 
 template <class St, bool GATHER, bool FIELDS>
-__global__ void __launch_bounds__(256, 4) step_kernel(StepArgs a) {
+__global__ void __launch_bounds__(256, St::min_blocks) step_kernel(StepArgs a) {
   chain_enter();
   step_tile<St, GATHER, FIELDS>(a, OfsTable{a}, a.slots, blockIdx, make_uint3(gridDim.x, gridDim.y, gridDim.z));
 }
