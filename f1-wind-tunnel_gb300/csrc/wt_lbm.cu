@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(256, St::min_blocks) step_kernel(StepArgs a) {
 // Many lattices in one launch: block b belongs to the lattice L with
 // tile_base[L] <= b < tile_base[L+1]; its coordinates follow that lattice's grid.
 template <class St, bool GATHER, bool FIELDS>
-__global__ void __launch_bounds__(256, 4) batch_step_kernel(const StepArgs* __restrict__ args,
+__global__ void __launch_bounds__(256, St::min_blocks) batch_step_kernel(const StepArgs* __restrict__ args,
                                                             const BatchTiles* __restrict__ tiles, uint32_t count,
                                                             uint32_t pending) {
   chain_enter();
