@@ -14,13 +14,16 @@
 #include "wt_internal.h"
 #include "wt_fields.h"
 #include "wt_render.h"
+#include "wt_mesh.h"
 #include "wt_lattice.cuh"
 
 using namespace wt;
 
 struct wt_renderer;
+struct wt_mesh;
 namespace {
 void release_renderer_buffers(wt_renderer* r);
+void release_mesh_buffers(wt_mesh* m);
 }
 
 struct wt_ctx {
@@ -87,6 +90,7 @@ struct wt_ctx {
   float4* car_rig = nullptr;
   uint32_t car_pdims[3] = {1, 1, 1};
   std::vector<wt_renderer*> renderers;     // live renderers over this lattice
+  std::vector<wt_mesh*> meshes;            // live car meshes on this context
   std::string err;
 };
 
@@ -504,6 +508,8 @@ int wt_destroy(wt_ctx* c) {
   // wt_render_destroy only frees the handle, and other calls on it fail.
   for (wt_renderer* r : c->renderers) release_renderer_buffers(r);
   c->renderers.clear();
+  for (wt_mesh* m : c->meshes) release_mesh_buffers(m);
+  c->meshes.clear();
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
                   c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters,
@@ -1291,9 +1297,45 @@ struct wt_renderer {
   ushort4* bloom_a = nullptr;
   ushort4* bloom_b = nullptr;
   uchar4* out = nullptr;
+  ushort4* g_albedo = nullptr;        // car G-buffer (engine.ts:297-303)
+  ushort4* g_normal = nullptr;
+  uchar4* g_material = nullptr;
   unsigned long long* acc = nullptr;  // glow fixed-point sums, w*h*4
   float4* staging = nullptr;          // host particle / line data copied for a draw
   size_t staging_bytes = 0;
+  // mesh pass scratch, made on the first wt_render_mesh: depth, visibility keys,
+  // decal counts / offsets / cursors (w*h each), grown buffers below
+  float* m_depth = nullptr;
+  unsigned long long* m_keys = nullptr;
+  uint32_t* m_dcount = nullptr;
+  uint32_t* m_doff = nullptr;
+  uint32_t* m_dcur = nullptr;
+  uint32_t* m_nbig = nullptr;
+  uint32_t* m_dslots = nullptr;
+  size_t m_slots_cap = 0;
+  float4* m_corners = nullptr;
+  size_t m_corners_cap = 0;
+  uint4* m_big = nullptr;
+  size_t m_big_cap = 0;
+  void* m_scan = nullptr;
+  size_t m_scan_bytes = 0;
+  wt::MeshDraw* m_draws = nullptr;
+  size_t m_draws_cap = 0;
+  float4* m_rig = nullptr;
+};
+
+struct wt_mesh {
+  wt_ctx* c = nullptr;
+  uint32_t n_verts = 0, n_indices = 0;
+  float4* verts = nullptr;
+  uint32_t* indices = nullptr;
+  uint8_t* tags = nullptr;
+  std::vector<uint8_t*> tex_data;          // device: each texture's levels back to back
+  std::vector<wtx::Level> levels;          // every level of every texture (device pointers)
+  std::vector<wt::MeshTex> texs;
+  wtx::Level* d_levels = nullptr;          // device copies of the two tables
+  wt::MeshTex* d_texs = nullptr;
+  std::vector<wt_mesh_draw> draws;
 };
 
 namespace {
@@ -1307,11 +1349,23 @@ int render_check(wt_renderer* r) {
   return check_ctx(r->c);
 }
 void release_renderer_buffers(wt_renderer* r) {
-  void* bufs[] = {r->scene, r->hist[0], r->hist[1], r->glow, r->bloom_a, r->bloom_b, r->out, r->acc, r->staging};
+  void* bufs[] = {r->scene,    r->hist[0],  r->hist[1],  r->glow,    r->bloom_a,   r->bloom_b, r->out,
+                  r->acc,      r->staging,  r->g_albedo, r->g_normal, r->g_material, r->m_depth, r->m_keys,
+                  r->m_dcount, r->m_doff,   r->m_dcur,   r->m_nbig,  r->m_dslots,  r->m_corners, r->m_big,
+                  r->m_scan,   r->m_draws,  r->m_rig};
   for (void* b : bufs)
     if (b) cudaFree(b);
-  r->scene = r->hist[0] = r->hist[1] = r->glow = r->bloom_a = r->bloom_b = nullptr;
-  r->out = nullptr;
+  r->m_depth = nullptr;
+  r->m_keys = nullptr;
+  r->m_dcount = r->m_doff = r->m_dcur = r->m_nbig = r->m_dslots = nullptr;
+  r->m_corners = nullptr;
+  r->m_big = nullptr;
+  r->m_scan = nullptr;
+  r->m_draws = nullptr;
+  r->m_rig = nullptr;
+  r->m_slots_cap = r->m_corners_cap = r->m_big_cap = r->m_scan_bytes = r->m_draws_cap = 0;
+  r->scene = r->hist[0] = r->hist[1] = r->glow = r->bloom_a = r->bloom_b = r->g_albedo = r->g_normal = nullptr;
+  r->out = r->g_material = nullptr;
   r->acc = nullptr;
   r->staging = nullptr;
   r->staging_bytes = 0;
@@ -1327,6 +1381,9 @@ void* target_ptr(wt_renderer* r, int t, size_t* bytes) {
     case WT_TARGET_BLOOM_A: *bytes = half * 8; return r->bloom_a;
     case WT_TARGET_BLOOM_B: *bytes = half * 8; return r->bloom_b;
     case WT_TARGET_OUTPUT: *bytes = full * 4; return r->out;
+    case WT_TARGET_GALBEDO: *bytes = full * 8; return r->g_albedo;
+    case WT_TARGET_GNORMAL: *bytes = full * 8; return r->g_normal;
+    case WT_TARGET_GMATERIAL: *bytes = full * 4; return r->g_material;
     default: *bytes = 0; return nullptr;
   }
 }
@@ -1386,6 +1443,9 @@ int wt_render_create(wt_ctx* c, uint32_t width, uint32_t height, wt_renderer** o
   alloc((void**)&r->bloom_b, half * 8);
   alloc((void**)&r->out, full * 4);
   alloc((void**)&r->acc, full * 32);
+  alloc((void**)&r->g_albedo, full * 8);
+  alloc((void**)&r->g_normal, full * 8);
+  alloc((void**)&r->g_material, full * 4);
   if (e != cudaSuccess) {
     release_renderer_buffers(r);
     delete r;
@@ -1402,8 +1462,6 @@ int wt_render_scene(wt_renderer* r, const wt_cam* cam, const wt_look* look, cons
   if (rc) return rc;
   wt_ctx* c = r->c;
   if (!cam || !look || !view) return fail(c, WT_ERR_ARG, "wt_render_scene: null argument");
-  if (look->mesh_mode != 0u)
-    return fail(c, WT_ERR_UNSUPPORTED, "wt_render_scene: the baked-mesh G-buffer path (mesh_mode) is not built");
   SceneArgs a;
   a.shape = c->shape;
   a.car = car_view(c);
@@ -1420,6 +1478,8 @@ int wt_render_scene(wt_renderer* r, const wt_cam* cam, const wt_look* look, cons
   a.surf_mode = look->surf_mode; a.palette = look->palette; a.carbon_body = look->carbon_body; a.is_f1 = look->is_f1;
   a.slice_axis = look->slice_axis; a.show_flow = look->show_flow;
   a.slice_pos = look->slice_pos; a.slice_alpha = look->slice_alpha;
+  a.mesh_mode = look->mesh_mode; a.cooling = look->cooling;
+  a.g_albedo = r->g_albedo; a.g_normal = r->g_normal; a.g_material = r->g_material;
   a.key = f3n(-0.32f, 0.90f, 0.30f);    // KEY (render-wgsl.ts:38)
   a.fill_a = f3n(0.6f, 0.35f, -0.7f);   // shadeSurface fill lights (render-wgsl.ts:265)
   a.fill_b = f3n(0.6f, 0.35f, 0.7f);
@@ -1561,5 +1621,286 @@ int wt_render_write(wt_renderer* r, int target, const void* host) {
   if (!p || !host) return fail(c, WT_ERR_ARG, "wt_render_write: unknown target or null buffer");
   WT_CUDA(c, cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, c->stream));
   WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WT_OK;
+}
+
+namespace {
+void release_mesh_buffers(wt_mesh* m) {
+  void* bufs[] = {m->verts, m->indices, m->tags, m->d_levels, m->d_texs};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  for (uint8_t* t : m->tex_data) cudaFree(t);
+  m->verts = nullptr;
+  m->indices = nullptr;
+  m->tags = nullptr;
+  m->d_levels = nullptr;
+  m->d_texs = nullptr;
+  m->tex_data.clear();
+  m->levels.clear();
+  m->texs.clear();
+  m->c = nullptr;
+}
+int mesh_check(wt_mesh* m) {
+  if (!m || !m->c) return WT_ERR_ARG;  // also: its context was destroyed
+  return check_ctx(m->c);
+}
+// halveRgba (mesh-car.ts:30-44): the next mip level, a rounded 2 x 2 box
+std::vector<uint8_t> halve_rgba(const std::vector<uint8_t>& src, uint32_t w, uint32_t h, uint32_t* ow, uint32_t* oh) {
+  const uint32_t nw = w >> 1 ? w >> 1 : 1, nh = h >> 1 ? h >> 1 : 1;
+  std::vector<uint8_t> out((size_t)nw * nh * 4);
+  for (uint32_t y = 0; y < nh; y++) {
+    const size_t y0 = std::min(h - 1, y * 2), y1 = std::min(h - 1, y * 2 + 1);
+    for (uint32_t x = 0; x < nw; x++) {
+      const size_t x0 = std::min(w - 1, x * 2), x1 = std::min(w - 1, x * 2 + 1);
+      for (int k = 0; k < 4; k++) {
+        const unsigned sum = src[(y0 * w + x0) * 4 + k] + src[(y0 * w + x1) * 4 + k] + src[(y1 * w + x0) * 4 + k] +
+                             src[(y1 * w + x1) * 4 + k] + 2u;
+        out[((size_t)y * nw + x) * 4 + k] = (uint8_t)(sum >> 2);
+      }
+    }
+  }
+  *ow = nw;
+  *oh = nh;
+  return out;
+}
+// grow a device buffer to at least `need` elements (contents not kept)
+template <class T>
+cudaError_t grow(T** p, size_t* cap, size_t need) {
+  if (*cap >= need && *p) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  const size_t n = need > 0 ? need : 1;
+  const cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+}  // namespace
+
+int wt_png_unfilter(const uint8_t* filtered, uint32_t rows, uint32_t row_bytes, uint32_t bpp, uint8_t* out) {
+  if (!filtered || !out || bpp == 0 || bpp > 8) return WT_ERR_ARG;
+  const uint8_t* src = filtered;
+  for (uint32_t y = 0; y < rows; y++, src += (size_t)row_bytes + 1) {
+    const uint8_t type = src[0];
+    const uint8_t* f = src + 1;
+    uint8_t* o = out + (size_t)y * row_bytes;
+    const uint8_t* up = y ? o - row_bytes : nullptr;
+    for (uint32_t i = 0; i < row_bytes; i++) {
+      const int a = i >= bpp ? o[i - bpp] : 0;  // left, above, above-left (0 outside the image)
+      const int b = up ? up[i] : 0;
+      const int c = (up && i >= bpp) ? up[i - bpp] : 0;
+      int pred;
+      switch (type) {
+        case 0: pred = 0; break;
+        case 1: pred = a; break;
+        case 2: pred = b; break;
+        case 3: pred = (a + b) >> 1; break;
+        case 4: {  // Paeth: the neighbour closest to a + b - c, ties to a, then b
+          const int p = a + b - c, pa = abs(p - a), pb = abs(p - b), pc = abs(p - c);
+          pred = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+          break;
+        }
+        default: return WT_ERR_ARG;
+      }
+      o[i] = (uint8_t)(f[i] + pred);
+    }
+  }
+  return WT_OK;
+}
+
+int wt_mesh_create(wt_ctx* c, const float* verts, uint32_t n_verts, const uint32_t* indices, uint32_t n_indices,
+                   const uint8_t* tags, wt_mesh** out) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!out) return fail(c, WT_ERR_ARG, "wt_mesh_create: null output");
+  *out = nullptr;
+  if (!verts || !indices || !tags || n_verts == 0 || n_indices == 0)
+    return fail(c, WT_ERR_ARG, "wt_mesh_create: empty or null vertex, index or tag buffer");
+  for (uint32_t i = 0; i < n_indices; i++)
+    if (indices[i] >= n_verts)
+      return fail(c, WT_ERR_ARG, "wt_mesh_create: index " + std::to_string(i) + " out of range");
+  wt_mesh* m = new wt_mesh;
+  m->c = c;
+  m->n_verts = n_verts;
+  m->n_indices = n_indices;
+  cudaError_t e = cudaMalloc((void**)&m->verts, (size_t)n_verts * 32);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->indices, (size_t)n_indices * 4);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->tags, n_verts);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->verts, verts, (size_t)n_verts * 32, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->indices, indices, (size_t)n_indices * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->tags, tags, n_verts, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    release_mesh_buffers(m);
+    delete m;
+    return fail(c, e == cudaErrorMemoryAllocation ? WT_ERR_NOMEM : WT_ERR_CUDA,
+                std::string("wt_mesh_create: ") + cudaGetErrorString(e));
+  }
+  c->meshes.push_back(m);
+  *out = m;
+  return WT_OK;
+}
+
+void wt_mesh_destroy(wt_mesh* m) {
+  if (!m) return;
+  if (wt_ctx* c = m->c) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (size_t i = 0; i < c->meshes.size(); i++)
+      if (c->meshes[i] == m) {
+        c->meshes.erase(c->meshes.begin() + (long)i);
+        break;
+      }
+    release_mesh_buffers(m);
+  }
+  delete m;
+}
+
+int wt_mesh_add_texture(wt_mesh* m, uint32_t width, uint32_t height, const uint8_t* rgba, int32_t* index) {
+  int rc = mesh_check(m);
+  if (rc) return rc;
+  wt_ctx* c = m->c;
+  if (!rgba || !index || width == 0 || height == 0 || width > 16384 || height > 16384)
+    return fail(c, WT_ERR_ARG, "wt_mesh_add_texture: null buffer or size not 1..16384");
+  // levels: floor(log2(max(w, h))) + 1 (mesh-car.ts:115)
+  uint32_t big = width > height ? width : height, n_levels = 0;
+  while (big) {
+    n_levels++;
+    big >>= 1;
+  }
+  std::vector<std::vector<uint8_t>> lv(1, std::vector<uint8_t>(rgba, rgba + (size_t)width * height * 4));
+  std::vector<uint32_t> ws{width}, hs{height};
+  size_t total = lv[0].size();
+  for (uint32_t l = 1; l < n_levels; l++) {
+    uint32_t nw, nh;
+    lv.push_back(halve_rgba(lv.back(), ws.back(), hs.back(), &nw, &nh));
+    ws.push_back(nw);
+    hs.push_back(nh);
+    total += lv.back().size();
+  }
+  uint8_t* d = nullptr;
+  WT_CUDA(c, cudaMalloc((void**)&d, total));
+  m->tex_data.push_back(d);
+  size_t off = 0;
+  wt::MeshTex t{(uint32_t)m->levels.size(), n_levels};
+  for (uint32_t l = 0; l < n_levels; l++) {
+    WT_CUDA(c, cudaMemcpyAsync(d + off, lv[l].data(), lv[l].size(), cudaMemcpyHostToDevice, c->stream));
+    m->levels.push_back(wtx::Level{d + off, (int)ws[l], (int)hs[l]});
+    off += lv[l].size();
+  }
+  m->texs.push_back(t);
+  // the tables, copied whole (they are small)
+  if (m->d_levels) cudaFree(m->d_levels);
+  if (m->d_texs) cudaFree(m->d_texs);
+  m->d_levels = nullptr;
+  m->d_texs = nullptr;
+  WT_CUDA(c, cudaMalloc((void**)&m->d_levels, m->levels.size() * sizeof(wtx::Level)));
+  WT_CUDA(c, cudaMalloc((void**)&m->d_texs, m->texs.size() * sizeof(wt::MeshTex)));
+  WT_CUDA(c, cudaMemcpyAsync(m->d_levels, m->levels.data(), m->levels.size() * sizeof(wtx::Level),
+                             cudaMemcpyHostToDevice, c->stream));
+  WT_CUDA(c, cudaMemcpyAsync(m->d_texs, m->texs.data(), m->texs.size() * sizeof(wt::MeshTex), cudaMemcpyHostToDevice,
+                             c->stream));
+  WT_CUDA(c, cudaStreamSynchronize(c->stream));
+  *index = (int32_t)m->texs.size() - 1;
+  return WT_OK;
+}
+
+int wt_mesh_add_draw(wt_mesh* m, const wt_mesh_draw* d) {
+  int rc = mesh_check(m);
+  if (rc) return rc;
+  wt_ctx* c = m->c;
+  if (!d) return fail(c, WT_ERR_ARG, "wt_mesh_add_draw: null draw");
+  if ((uint64_t)d->first_index + d->count > m->n_indices)
+    return fail(c, WT_ERR_ARG, "wt_mesh_add_draw: index range beyond the index buffer");
+  if (d->has_tex > 0.5f && (d->texture < 0 || d->texture >= (int32_t)m->texs.size()))
+    return fail(c, WT_ERR_ARG, "wt_mesh_add_draw: has_tex set without a valid texture");
+  m->draws.push_back(*d);
+  return WT_OK;
+}
+
+int wt_render_mesh(wt_renderer* r, wt_mesh* m, const wt_mesh_cam* cam, const wt_rig* rig, int optional) {
+  int rc = render_check(r);
+  if (rc) return rc;
+  wt_ctx* c = r->c;
+  if (!m || m->c != c) return fail(c, WT_ERR_ARG, "wt_render_mesh: mesh missing or made on another context");
+  if (!cam || !rig) return fail(c, WT_ERR_ARG, "wt_render_mesh: null camera or rig");
+  // the draws of this frame in record order, with their corner and triangle bases
+  std::vector<wt::MeshDraw> dl;
+  uint64_t corners = 0, tris = 0;
+  for (const wt_mesh_draw& d : m->draws) {
+    if (d.optional && !optional) continue;
+    wt::MeshDraw x{};
+    for (int k = 0; k < 4; k++) x.color[k] = d.color[k];
+    x.metal = d.metal; x.rough = d.rough; x.coat = d.coat; x.alpha_cut = d.alpha_cut;
+    x.emissive = d.emissive; x.has_tex = d.has_tex; x.is_body = d.is_body;
+    x.first_index = d.first_index;
+    x.count = d.count - d.count % 3u;
+    x.tex = d.has_tex > 0.5f ? d.texture : -1;
+    x.blend = d.blend ? 1u : 0u;
+    x.corner_base = (uint32_t)corners;
+    x.tri_base = (uint32_t)tris;
+    corners += x.count;
+    tris += x.count / 3u;
+    dl.push_back(x);
+  }
+  if (tris >= 0x7fffffffull || corners >= 0xffffffffull)
+    return fail(c, WT_ERR_ARG, "wt_render_mesh: more than 2^31 - 1 triangles");
+  const size_t px = (size_t)r->w * r->h;
+  if (!r->m_depth) {  // per-pixel scratch, once per renderer
+    WT_CUDA(c, cudaMalloc((void**)&r->m_depth, px * 4));
+    WT_CUDA(c, cudaMalloc((void**)&r->m_keys, px * 8));
+    WT_CUDA(c, cudaMalloc((void**)&r->m_dcount, px * 4));
+    WT_CUDA(c, cudaMalloc((void**)&r->m_doff, px * 4));
+    WT_CUDA(c, cudaMalloc((void**)&r->m_dcur, px * 4));
+    WT_CUDA(c, cudaMalloc((void**)&r->m_nbig, 4));
+  }
+  WT_CUDA(c, grow(&r->m_corners, &r->m_corners_cap, (size_t)corners * 3));
+  WT_CUDA(c, grow(&r->m_big, &r->m_big_cap, (size_t)tris * 2));
+  WT_CUDA(c, grow(&r->m_draws, &r->m_draws_cap, dl.size()));
+  if (!dl.empty())  // pageable source: copied before the call returns
+    WT_CUDA(c, cudaMemcpyAsync(r->m_draws, dl.data(), dl.size() * sizeof(wt::MeshDraw), cudaMemcpyHostToDevice,
+                               c->stream));
+  wt::MeshArgs a{};
+  a.verts = m->verts; a.indices = m->indices; a.tags = m->tags;
+  a.levels = m->d_levels; a.texs = m->d_texs;
+  a.draws = r->m_draws; a.n_draws = (uint32_t)dl.size();
+  for (int k = 0; k < 16; k++) a.vp[k] = cam->view_proj[k];
+  for (int k = 0; k < 3; k++) a.cam_pos[k] = cam->cam_pos[k];
+  a.ride_h = cam->ride_h; a.jitter[0] = cam->jitter[0]; a.jitter[1] = cam->jitter[1];
+  a.rake = cam->rake; a.base_ride = cam->base_ride;
+  // the mesh's rig travels in its own copy so the scene's car model stays as set
+  if (!r->m_rig) WT_CUDA(c, cudaMalloc((void**)&r->m_rig, sizeof(wt_rig)));
+  WT_CUDA(c, cudaMemcpyAsync(r->m_rig, rig, sizeof(wt_rig), cudaMemcpyHostToDevice, c->stream));
+  a.rig = r->m_rig;
+  a.w = r->w; a.h = r->h;
+  a.corners = r->m_corners;
+  a.depth = r->m_depth; a.keys = r->m_keys;
+  a.big = r->m_big; a.n_big = r->m_nbig; a.big_cap = (uint32_t)std::min<size_t>(r->m_big_cap, 0xffffffffu);
+  a.g_albedo = r->g_albedo; a.g_normal = r->g_normal; a.g_material = r->g_material;
+  a.dcount = r->m_dcount; a.doff = r->m_doff; a.dcur = r->m_dcur; a.dslots = r->m_dslots;
+  WT_CUDA(c, launch_mesh_clear(a, c->stream));
+  WT_CUDA(c, launch_mesh_vertex(a, (uint32_t)corners, c->stream));
+  for (size_t i = 0; i < dl.size();) {  // runs of opaque draws and runs of decals
+    size_t j = i;
+    while (j < dl.size() && dl[j].blend == dl[i].blend) j++;
+    const uint32_t tri0 = dl[i].tri_base, tri1 = dl[j - 1].tri_base + dl[j - 1].count / 3u;
+    if (!dl[i].blend) {
+      WT_CUDA(c, launch_mesh_opaque(a, (uint32_t)i, (uint32_t)j, tri0, tri1, c->stream));
+    } else if (tri1 > tri0) {
+      WT_CUDA(c, launch_mesh_decal_count(a, (uint32_t)i, (uint32_t)j, tri0, tri1, c->stream));
+      size_t need = 0;
+      WT_CUDA(c, launch_mesh_decal_scan(a, nullptr, &need, c->stream));
+      WT_CUDA(c, grow((uint8_t**)&r->m_scan, &r->m_scan_bytes, need));
+      WT_CUDA(c, launch_mesh_decal_scan(a, r->m_scan, &need, c->stream));
+      uint32_t last[2] = {0, 0};
+      WT_CUDA(c, cudaMemcpyAsync(&last[0], r->m_doff + px - 1, 4, cudaMemcpyDeviceToHost, c->stream));
+      WT_CUDA(c, cudaMemcpyAsync(&last[1], r->m_dcount + px - 1, 4, cudaMemcpyDeviceToHost, c->stream));
+      WT_CUDA(c, cudaStreamSynchronize(c->stream));
+      WT_CUDA(c, grow(&r->m_dslots, &r->m_slots_cap, (size_t)last[0] + last[1]));
+      a.dslots = r->m_dslots;
+      WT_CUDA(c, launch_mesh_decal_blend(a, (uint32_t)i, (uint32_t)j, tri0, tri1, c->stream));
+    }
+    i = j;
+  }
   return WT_OK;
 }

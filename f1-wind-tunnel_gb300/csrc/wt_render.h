@@ -28,6 +28,12 @@ struct SceneArgs {
   F3 bmin, bmax, paint_lin, accent_lin;
   uint32_t surf_mode, palette, carbon_body, is_f1, slice_axis, show_flow;
   float slice_pos, slice_alpha;
+  uint32_t mesh_mode, cooling;  // meshMode: surfaces come from the G-buffer below
+  // car G-buffer of the mesh pass (engine.ts:297-303), w x h: albedo (rgb, rough)
+  // and normal-distance as binary16, material (metal, coat, emissive, 1) as RGBA8
+  const ushort4* g_albedo;
+  const ushort4* g_normal;
+  const uchar4* g_material;
   // normalize(KEY) and the two fill-light directions of shadeSurface
   F3 key, fill_a, fill_b;
   uint32_t w, h;

@@ -329,7 +329,7 @@ __device__ float f1_emission(const Scene& S, V3 pw) {
 constexpr float W17_H = 0.015f, W17_BASE_RIDE = 0.092f;
 constexpr int RIG_HINGES = 71, RIG_ANGLES = 72, RIG_EXTRA = 73, RIG_FLY = 74, RIG_GRIDS = 75;
 
-__device__ __forceinline__ float4 rig_at(const Scene& S, int i) { return __ldg(S.car.rig + i); }
+__device__ __forceinline__ float4 rig_at(const float4* R, int i) { return __ldg(R + i); }
 __device__ __forceinline__ float half_at(const uint16_t* t, size_t i) {
   return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(t) + i)));
 }
@@ -365,28 +365,28 @@ __device__ float rig_weight(uint32_t part, float z) {
   }
   return (part == 3u || part == 4u) ? 1.0f : 0.0f;
 }
-__device__ V2 rig_hinge(const Scene& S, uint32_t part, float z) {
-  if (part == 3u) { const float4 g = rig_at(S, RIG_HINGES); return v2(g.z, g.w); }
-  if (part == 4u) { const float4 g = rig_at(S, RIG_HINGES); return v2(g.x, g.y); }
+__device__ V2 rig_hinge(const float4* R, uint32_t part, float z) {
+  if (part == 3u) { const float4 g = rig_at(R, RIG_HINGES); return v2(g.z, g.w); }
+  if (part == 4u) { const float4 g = rig_at(R, RIG_HINGES); return v2(g.x, g.y); }
   const float f = clmp(ab(z) / 0.01f, 0.0f, 70.0f);
   const uint32_t i = (uint32_t)floorf(f);
   const uint32_t j = (i + 1u) < 70u ? i + 1u : 70u;
-  const float4 a = rig_at(S, (int)i), b = rig_at(S, (int)j);
+  const float4 a = rig_at(R, (int)i), b = rig_at(R, (int)j);
   const float t = f - (float)i;
   return part == 1u ? mix2(v2(a.x, a.y), v2(b.x, b.y), t) : mix2(v2(a.z, a.w), v2(b.z, b.w), t);
 }
-__device__ float rig_angle(const Scene& S, uint32_t part, float z) {
-  const float4 an = rig_at(S, RIG_ANGLES);
+__device__ float rig_angle(const float4* R, uint32_t part, float z) {
+  const float4 an = rig_at(R, RIG_ANGLES);
   float a = 0.0f;
   if (part == 1u) a = an.x;
   else if (part == 2u) a = an.y;
   else if (part == 3u) a = an.z;
   else if (part == 4u) a = an.w;
-  if (part == 3u || part == 4u) a = a + rig_at(S, RIG_EXTRA).x * sstep(0.12f, 0.48f, ab(z));
+  if (part == 3u || part == 4u) a = a + rig_at(R, RIG_EXTRA).x * sstep(0.12f, 0.48f, ab(z));
   return a * rig_weight(part, z);
 }
-__device__ float rig_scale(const Scene& S, uint32_t part) {
-  const float ey = rig_at(S, RIG_EXTRA).y;
+__device__ float rig_scale(const float4* R, uint32_t part) {
+  const float ey = rig_at(R, RIG_EXTRA).y;
   if (part == 3u) return ey;
   if (part == 1u || part == 2u) return 1.0f - (1.0f - ey) * 0.65f;
   return 1.0f;
@@ -394,9 +394,9 @@ __device__ float rig_scale(const Scene& S, uint32_t part) {
 // rigRotate with dir = -1 (the distance field's direction)
 __device__ V3 rig_rotate_back(const Scene& S, V3 p, uint32_t part) {
   if (part == 0u || part > 4u) return p;
-  const float a = rig_angle(S, part, p.z) * -1.0f;
-  const float k = rig_scale(S, part);
-  const V2 h = rig_hinge(S, part, p.z);
+  const float a = rig_angle(S.car.rig, part, p.z) * -1.0f;
+  const float k = rig_scale(S.car.rig, part);
+  const V2 h = rig_hinge(S.car.rig, part, p.z);
   const float c = wtm::cosf(a), s = wtm::sinf(a);
   V2 d = v2(p.x, p.y) - h;
   d = v2(c * d.x - s * d.y, s * d.x + c * d.y);
@@ -409,7 +409,7 @@ __device__ float pod_weight(V3 p) {
          (1.0f - sstep(0.6f, 0.7f, p.y)) * sstep(0.26f, 0.4f, ab(p.z));
 }
 __device__ V3 pod_deform_back(const Scene& S, V3 p) {
-  const float c = rig_at(S, RIG_EXTRA).z * pod_weight(p);
+  const float c = rig_at(S.car.rig, RIG_EXTRA).z * pod_weight(p);
   if (c <= 0.0f) return p;
   const float az = ab(p.z);
   const float kz = dv(1.0f, 1.0f - c);
@@ -435,7 +435,7 @@ __device__ float sd_w17_body(const Scene& S, V3 p) {
 }
 // sdW17Part (f1.ts:342-353)
 __device__ __noinline__ float sd_w17_part(const Scene& S, V3 pb, uint32_t part) {
-  const float4 g0 = rig_at(S, RIG_GRIDS + (int)(part - 1u) * 2), g1 = rig_at(S, RIG_GRIDS + (int)(part - 1u) * 2 + 1);
+  const float4 g0 = rig_at(S.car.rig, RIG_GRIDS + (int)(part - 1u) * 2), g1 = rig_at(S.car.rig, RIG_GRIDS + (int)(part - 1u) * 2 + 1);
   const V3 q = rig_rotate_back(S, pb, part);
   const V3 ext = v3((g1.x - 1.0f) * g0.w, (g1.y - 1.0f) * g0.w, (g1.z - 1.0f) * g0.w);
   const V3 half = ext * 0.5f;
@@ -444,16 +444,16 @@ __device__ __noinline__ float sd_w17_part(const Scene& S, V3 pb, uint32_t part) 
   const V3 cell = v3(dv(q.x - g0.x, g0.w), dv(q.y - g0.y, g0.w), dv(q.z - g0.z, g0.w));
   const float ax = (float)S.car.pdims[0], ay = (float)S.car.pdims[1], az = (float)S.car.pdims[2];
   const V3 uvw = v3(dv(cell.x + 0.5f, ax), dv(cell.y + 0.5f, ay), dv(cell.z + g1.w + 0.5f, az));
-  const float sc = rig_scale(S, part);
+  const float sc = rig_scale(S.car.rig, part);
   return sample3(S.car.parts, (int)S.car.pdims[0], (int)S.car.pdims[1], (int)S.car.pdims[2], uvw) * mn(sc, 1.0f);
 }
 // sdW17 (f1.ts:354-369)
 __device__ V2 sd_w17(const Scene& S, V3 pw) {
   const V3 pa = v3(pw.x, pw.y, ab(pw.z));
   const V3 p = w17_body_frame(S, pa);
-  const float squeeze = 1.0f - rig_at(S, RIG_EXTRA).z * pod_weight(p);
+  const float squeeze = 1.0f - rig_at(S.car.rig, RIG_EXTRA).z * pod_weight(p);
   V2 res = v2(sd_w17_body(S, pod_deform_back(S, p)) * 0.95f * squeeze, 12.0f);
-  const float4 fly = rig_at(S, RIG_FLY);
+  const float4 fly = rig_at(S.car.rig, RIG_FLY);
   if (fly.z > 0.5f && p.x < 0.85f && p.y < 0.6f)
     res = op_u(res, v2(mn(mn(sd_w17_part(S, p, 1u), sd_w17_part(S, p, 2u)), sd_w17_part(S, p, 5u)) * 0.95f, 7.0f));
   if (fly.w > 0.5f && p.x > 4.4f && p.y > 0.5f)

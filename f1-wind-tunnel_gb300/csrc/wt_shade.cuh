@@ -38,6 +38,11 @@ __device__ __forceinline__ V3 nrm3(V3 a) {
 // reflect(e1, e2) = e1 - 2 dot(e2, e1) e2
 __device__ __forceinline__ V3 reflect3(V3 e1, V3 e2) { return e1 - (2.0f * dot3(e2, e1)) * e2; }
 __device__ __forceinline__ float fractf(float x) { return x - floorf(x); }
+// an RGBA binary16 texel
+__device__ __forceinline__ float4 h4(ushort4 v) {
+  return make_float4(__half2float(__ushort_as_half(v.x)), __half2float(__ushort_as_half(v.y)),
+                     __half2float(__ushort_as_half(v.z)), __half2float(__ushort_as_half(v.w)));
+}
 __device__ __forceinline__ float stepf(float edge, float x) { return edge <= x ? 1.0f : 0.0f; }
 __device__ __forceinline__ V3 c3(const F3& f) { return v3(f.x, f.y, f.z); }
 __device__ __forceinline__ uint32_t mn_u(uint32_t a, uint32_t b) { return b < a ? b : a; }
@@ -248,7 +253,29 @@ __device__ Mat livery_body(const Scene& S, V3 p, float b, V3 silver, V3 teal) {
   return gloss_black();
 }
 
-// materialAt (render-wgsl.ts:180-255) for the analytic scenes (look.meshMode == 0).
+// louvres (render-wgsl.ts:160-178): cooling slots painted onto the mesh's bodywork.
+__device__ Mat louvres(const SceneArgs& a, V3 p, V3 n, const Mat mt) {
+  if (a.cooling == 0u) return mt;
+  const bool open = a.cooling == 2u;
+  const float az = ab(p.z);
+  float slot = 0.0f;
+  const float x0 = open ? 3.05f : 3.35f;
+  const float x1 = open ? 3.95f : 3.85f;
+  if (p.x > x0 && p.x < x1 && az > 0.16f && az < 0.48f && p.y > 0.45f && n.y > 0.55f) {
+    const float f = fractf(p.x / 0.045f);
+    slot = ((open ? 0.55f : 0.32f) >= f ? 1.0f : 0.0f) * sstep(0.16f, 0.2f, az) * (1.0f - sstep(0.44f, 0.48f, az));
+  }
+  if (open && p.x > 3.6f && p.x < 4.25f && az > 0.08f && az < 0.32f && p.y > 0.5f && p.y < 0.8f && ab(n.z) > 0.5f) {
+    slot = mx(slot, (0.4f >= fractf(p.x / 0.05f) ? 1.0f : 0.0f) * sstep(0.52f, 0.56f, p.y) *
+                        (1.0f - sstep(0.74f, 0.78f, p.y)));
+  }
+  if (slot <= 0.0f) return mt;
+  return mat(vmix3(mt.albedo, v3(0.004f, 0.004f, 0.004f), slot), mixf(mt.rough, 0.9f, slot), mt.metal * (1.0f - slot),
+             mt.coat * (1.0f - slot), mt.emit);
+}
+
+// materialAt (render-wgsl.ts:180-255).  With the baked mesh (meshMode) only
+// reflections reach it past the wings: a neutral dark body stands in.
 __device__ __noinline__ Mat material_at(const Scene& S, const SceneArgs& a, float m, V3 pw, V3 n, float vd) {
   const V3 pabs = v3(pw.x, pw.y, ab(pw.z));
   const V3 p = a.is_f1 != 0u ? body_frame(S, pabs) : pabs;
@@ -308,6 +335,7 @@ __device__ __noinline__ Mat material_at(const Scene& S, const SceneArgs& a, floa
     if (p.z > 0.495f && p.y > b + rear_endplate_top(S) - 0.06f) return paint_mat(accent);
     return carbon_mat(p, n, vd);
   }
+  if (a.mesh_mode != 0u) return mat(v3(0.02f, 0.021f, 0.024f), 0.3f, 0.0f, 0.8f, zero3());
   if (m > 11.5f) return mat(v3(0.02f, 0.021f, 0.024f), 0.3f, 0.0f, 0.8f, zero3());
   if (m < 9.5f && m > 8.5f) {
     const bool front = pabs.x < 2.7f;
@@ -324,11 +352,11 @@ __device__ __noinline__ Mat material_at(const Scene& S, const SceneArgs& a, floa
   return mat(v3(0.3f, 0.0f, 0.0f), 0.2f, 0.0f, 1.0f, v3(4.0f, 0.12f, 0.08f));
 }
 
-// shadeSurface (render-wgsl.ts:257-283); lift = 0.004 without the baked mesh
+// shadeSurface (render-wgsl.ts:257-283)
 __device__ __noinline__ V3 shade_surface(const Scene& S, const SceneArgs& a, V3 p, V3 n, V3 rd, const Mat mt, bool fast) {
   const V3 key = c3(a.key);
   float sh = 1.0f, ao = 1.0f;
-  const float lift = 0.004f;
+  const float lift = a.mesh_mode != 0u ? 0.045f : 0.004f;
   if (!fast) {
     sh = soft_shadow(S, a, p + n * lift, key);
     ao = ambient_occ(S, a, p + n * (lift - 0.004f), n);
@@ -365,15 +393,41 @@ __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, u
 
   V3 col = backdrop(rd);
   float t_hit = FAR;
-  const V2 hit = march(S, a, ro, rd, 220);
+  V2 hit = v2(FAR, 0.0f);
+  float4 gn = make_float4(0.0f, 0.0f, 0.0f, 0.0f), ga = gn, gm = gn;
+  if (a.mesh_mode != 0u) {
+    // the G-buffer texel under the pixel (it has the scene's size)
+    const int gx0 = to_i32(ux * (float)a.w), gy0 = to_i32(uy * (float)a.h);
+    const int gx = gx0 < 0 ? 0 : (gx0 > (int)a.w - 1 ? (int)a.w - 1 : gx0);
+    const int gy = gy0 < 0 ? 0 : (gy0 > (int)a.h - 1 ? (int)a.h - 1 : gy0);
+    const size_t gi = (size_t)gy * a.w + (size_t)gx;
+    gn = h4(a.g_normal[gi]);
+    if (gn.w > 0.0f) {
+      hit = v2(gn.w, 12.0f);
+      ga = h4(a.g_albedo[gi]);
+      const uchar4 m8 = a.g_material[gi];
+      gm = make_float4((float)m8.x / 255.0f, (float)m8.y / 255.0f, (float)m8.z / 255.0f, (float)m8.w / 255.0f);
+    }
+  } else {
+    hit = march(S, a, ro, rd, 220);
+  }
   float t_ground = FAR;
   if (rd.y < -1e-4f) t_ground = -ro.y / rd.y;
 
   if (hit.x < t_ground && hit.x < FAR) {
     const V3 p = ro + rd * hit.x;
     const float vd = hit.x;
-    const V3 n = calc_normal(S, a, p);
-    Mat mt = material_at(S, a, hit.y, p, n, vd);
+    V3 n;
+    Mat mt;
+    if (a.mesh_mode != 0u) {
+      n = nrm3(v3(gn.x, gn.y, gn.z));
+      if (dot3(n, rd) > 0.0f) n = -n;
+      const V3 alb = v3(ga.x, ga.y, ga.z);
+      mt = louvres(a, p, n, mat(alb, ga.w, gm.x, gm.y, alb * gm.z));
+    } else {
+      n = calc_normal(S, a, p);
+      mt = material_at(S, a, hit.y, p, n, vd);
+    }
     if (a.surf_mode == 1u) {
       V3 probe = p + n * a.g.h * 0.8f;
       Sample s = sample_flow(a.g, probe);

@@ -151,7 +151,21 @@ class Post(ctypes.Structure):
     _fields_ = [("bloom", _F), ("exposure", _F), ("pad0", _F), ("pad1", _F)]
 
 
-TARGET_SCENE, TARGET_HIST0, TARGET_HIST1, TARGET_GLOW, TARGET_BLOOM_A, TARGET_BLOOM_B, TARGET_OUTPUT = range(7)
+class MeshDraw(ctypes.Structure):
+    """wt_mesh_draw: the MeshMat uniform (render-wgsl.ts:653-657), then count, texture, blend, optional."""
+    _fields_ = [("color", _F * 4), ("metal", _F), ("rough", _F), ("coat", _F), ("alpha_cut", _F), ("emissive", _F),
+                ("has_tex", _F), ("is_body", _F), ("first_index", _U), ("count", _U), ("texture", ctypes.c_int32),
+                ("blend", _U), ("optional", _U)]
+
+
+class MeshCam(ctypes.Structure):
+    """MeshCam uniform (render-wgsl.ts:648-652)."""
+    _fields_ = [("view_proj", _F * 16), ("cam_pos", _F * 3), ("ride_h", _F), ("jitter", _F * 2), ("rake", _F),
+                ("base_ride", _F)]
+
+
+(TARGET_SCENE, TARGET_HIST0, TARGET_HIST1, TARGET_GLOW, TARGET_BLOOM_A, TARGET_BLOOM_B, TARGET_OUTPUT,
+ TARGET_GALBEDO, TARGET_GNORMAL, TARGET_GMATERIAL) = range(10)
 
 _vp = ctypes.c_void_p
 _PROTOS = {
@@ -200,6 +214,13 @@ _PROTOS = {
     "wt_render_present": (ctypes.c_int, [_vp, ctypes.POINTER(Post), ctypes.c_int]),
     "wt_render_read": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "wt_render_write": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "wt_mesh_create": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp, ctypes.c_uint32, _vp, ctypes.POINTER(_vp)]),
+    "wt_mesh_destroy": (None, [_vp]),
+    "wt_mesh_add_texture": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp,
+                                           ctypes.POINTER(ctypes.c_int32)]),
+    "wt_mesh_add_draw": (ctypes.c_int, [_vp, ctypes.POINTER(MeshDraw)]),
+    "wt_render_mesh": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(MeshCam), _vp, ctypes.c_int]),
+    "wt_png_unfilter": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
 }
 
 _lib = None

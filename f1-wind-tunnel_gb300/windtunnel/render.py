@@ -19,12 +19,13 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from ._abi import (TARGET_BLOOM_A, TARGET_BLOOM_B, TARGET_GLOW, TARGET_HIST0, TARGET_HIST1, TARGET_OUTPUT,
-                   TARGET_SCENE, Cam, Look, PDraw, Post, SDraw, Taa)
+from ._abi import (TARGET_BLOOM_A, TARGET_BLOOM_B, TARGET_GALBEDO, TARGET_GLOW, TARGET_GMATERIAL, TARGET_GNORMAL,
+                   TARGET_HIST0, TARGET_HIST1, TARGET_OUTPUT, TARGET_SCENE, Cam, Look, PDraw, Post, SDraw, Taa)
 
 __all__ = ["CameraState", "orbit_camera", "halton", "shape_bounds", "make_look", "FrameState", "FrameUniforms",
            "Renderer", "TARGET_SCENE",
-           "TARGET_HIST0", "TARGET_HIST1", "TARGET_GLOW", "TARGET_BLOOM_A", "TARGET_BLOOM_B", "TARGET_OUTPUT"]
+           "TARGET_HIST0", "TARGET_HIST1", "TARGET_GLOW", "TARGET_BLOOM_A", "TARGET_BLOOM_B", "TARGET_OUTPUT",
+           "TARGET_GALBEDO", "TARGET_GNORMAL", "TARGET_GMATERIAL"]
 
 STREAM_STEPS = 360  # engine.ts:28
 
@@ -193,6 +194,7 @@ class FrameUniforms:
     pdraw: object
     sdraw: object
     post: Post
+    halton: tuple = (0.0, 0.0)  # the frame's (jx, jy) before scaling to pixels
 
 
 class FrameState:
@@ -224,7 +226,7 @@ class FrameState:
                                                       lines.shape[1])
         post = Post()
         post.bloom, post.exposure = 0.75, 1.0  # engine.ts:324
-        return FrameUniforms(c, taa, cur, pd, sd, post)
+        return FrameUniforms(c, taa, cur, pd, sd, post, (jx, jy))
 
 
 class Renderer:
@@ -279,10 +281,11 @@ class Renderer:
 
     def _shape(self, target):
         w, h = self.half if target in (TARGET_BLOOM_A, TARGET_BLOOM_B) else self.size
-        return (h, w, 4), (np.uint8 if target == TARGET_OUTPUT else np.float16)
+        return (h, w, 4), (np.uint8 if target in (TARGET_OUTPUT, TARGET_GMATERIAL) else np.float16)
 
     def read(self, target):
-        """A target as [h, w, 4]: float16 for the float targets, uint8 for the output."""
+        """A target as [h, w, 4]: float16 for the float targets, uint8 for the output
+        and the G-buffer's material target."""
         shape, dt = self._shape(target)
         out = np.empty(shape, dt)
         self._check(self.lib.wt_render_read(self.r, target, out.ctypes.data), "wt_render_read")
@@ -293,12 +296,25 @@ class Renderer:
         arr = np.ascontiguousarray(data, dt).reshape(shape)
         self._check(self.lib.wt_render_write(self.r, target, arr.ctypes.data), "wt_render_write")
 
+    def mesh(self, mesh_car, cam, rig, gurney=False):
+        """The car mesh G-buffer pass (engine.ts:716): mesh_car a mesh_car.MeshCar,
+        cam its MeshCam uniform, rig the [87, 4] Rig uniform."""
+        mesh_car.record(self, cam, rig, gurney)
+
     # -- the frame's render passes (engine.ts:575-584, 660-725) ----------------
     def frame(self, cam, look, view, dt=1.0 / 60, kmh=250.0, parts=None, color_mode=0, smoke=True, lines=None,
-              flow_time=0.0, vortices=False):
+              flow_time=0.0, vortices=False, mesh=None, rig=None, params=None):
         """Scene, TAA resolve, glow (particles and/or streamlines), bloom and
-        present; returns the FrameUniforms used (u.cur = the history resolved into)."""
+        present; returns the FrameUniforms used (u.cur = the history resolved into).
+        With a car mesh (mesh_car.MeshCar, its Rig uniform and the ShapeParams of
+        the W17 scene) the G-buffer pass runs first and the scene pass takes the
+        car's surfaces from it (meshMode, engine.ts:679-686, 703, 716)."""
         u = self.state.next(cam, self.size, dt, kmh, parts, color_mode, smoke, lines, flow_time, vortices)
+        if mesh is not None:
+            from .mesh_car import mesh_cam
+            self.mesh(mesh, mesh_cam(cam, self.size, u.halton, params), rig, bool(getattr(params, "gurney", False)))
+            look = Look.from_buffer_copy(look)
+            look.mesh_mode = 1
         self.scene(u.cam, look, view)
         self.taa(u.taa, u.cur)
         self.glow(parts, u.pdraw, lines, u.sdraw)

@@ -295,8 +295,9 @@ int wt_streamlines(wt_ctx* ctx, const wt_stream_params* s, const wt_view* v, flo
  * The uniform structs below have the layouts of the WGSL uniforms they replace.
  * A renderer reads the fields and temperatures of its context's last step call
  * and the shape of its last wt_voxelize; its passes are queued on the
- * context's stream and return at once.  The baked-mesh G-buffer path
- * (look.mesh_mode != 0) is not built. */
+ * context's stream and return at once.  With look.mesh_mode != 0 the scene
+ * pass takes the car's surfaces from the renderer's G-buffer (the targets
+ * WT_TARGET_G*, written by wt_render_mesh or wt_render_write). */
 
 /* Cam uniform (render-wgsl.ts:5-11). */
 typedef struct wt_cam {
@@ -356,7 +357,11 @@ enum {
   WT_TARGET_GLOW = 3,    /* width x height, particles and streamlines */
   WT_TARGET_BLOOM_A = 4, /* half size, horizontal blur */
   WT_TARGET_BLOOM_B = 5, /* half size, vertical blur */
-  WT_TARGET_OUTPUT = 6   /* width x height, presented RGBA8 */
+  WT_TARGET_OUTPUT = 6,  /* width x height, presented RGBA8 */
+  /* the car G-buffer (engine.ts:297-303), width x height; cleared to 0 at creation */
+  WT_TARGET_GALBEDO = 7,  /* binary16: albedo rgb, roughness (or decal alpha) */
+  WT_TARGET_GNORMAL = 8,  /* binary16: normal xyz, distance to the camera (0 = no car) */
+  WT_TARGET_GMATERIAL = 9 /* RGBA8 unorm: metal, coat, emissive, 1 */
 };
 
 typedef struct wt_renderer wt_renderer;
@@ -364,7 +369,9 @@ typedef struct wt_renderer wt_renderer;
 /* Targets of one view: width x height (half-size bloom targets, at least 1x1). */
 int wt_render_create(wt_ctx* ctx, uint32_t width, uint32_t height, wt_renderer** out);
 void wt_render_destroy(wt_renderer* r);
-/* RENDER pass (render-wgsl.ts:288-398) into WT_TARGET_SCENE. */
+/* RENDER pass (render-wgsl.ts:288-398) into WT_TARGET_SCENE; look->mesh_mode
+ * selects the G-buffer composite (render-wgsl.ts:300-323), look->cooling the
+ * louvres painted on the mesh (0 closed, 1 partly, 2 fully open). */
 int wt_render_scene(wt_renderer* r, const wt_cam* cam, const wt_look* look, const wt_view* view);
 /* TAA resolve (render-wgsl.ts:456-518): scene and history 1-cur into history cur. */
 int wt_render_taa(wt_renderer* r, const wt_taa* taa, int cur);
@@ -383,6 +390,59 @@ int wt_render_present(wt_renderer* r, const wt_post* post, int cur);
 /* Copy a target to / from host memory (synchronous). */
 int wt_render_read(wt_renderer* r, int target, void* host);
 int wt_render_write(wt_renderer* r, int target, const void* host);
+
+/* ---- the car mesh G-buffer pass: MESH_DRAW (render-wgsl.ts:647-760) over the
+ * draws of MeshCar (mesh-car.ts:46-213), into the renderer's G-buffer
+ * (engine.ts:297-303, 716).  The depth test, decal blending and texture
+ * filtering rules are written out in wt_mesh.cu and wt_texfilter.h. */
+typedef struct wt_mesh wt_mesh;
+
+/* One draw (mesh-car.ts:134-175): the MeshMat uniform (render-wgsl.ts:653-657)
+ * in its first 12 words, then the draw's index-list entries, texture and state. */
+typedef struct wt_mesh_draw {
+  float color[4];
+  float metal, rough, coat, alpha_cut;
+  float emissive, has_tex, is_body; uint32_t first_index;
+  uint32_t count;    /* index-list entries drawn (count / 3 triangles) */
+  int32_t texture;   /* wt_mesh_add_texture index; -1 = none (has_tex must be 0) */
+  uint32_t blend;    /* decal (DECAL_BLEND): depth bias -4 / slope -1, 'less-equal', no
+                        depth write, albedo blended, the other targets kept */
+  uint32_t optional; /* drawn only when wt_render_mesh gets optional != 0 (the gurney) */
+} wt_mesh_draw;
+
+/* MeshCam uniform (render-wgsl.ts:648-652); view_proj column-major. */
+typedef struct wt_mesh_cam {
+  float view_proj[16];
+  float cam_pos[3], ride_h;
+  float jitter[2], rake, base_ride;
+} wt_mesh_cam;
+
+/* The vertex and index buffers of MeshCar.load (mesh-car.ts:63-95): verts n_verts
+ * x 8 floats (x, y, z, u, nx, ny, nz, v in the car frame), indices n_indices
+ * entries < n_verts, tags one byte per vertex (part in bits 0-2, assembly in
+ * bits 3-7, car-model.ts:44-50).  Copied to the device. */
+int wt_mesh_create(wt_ctx* ctx, const float* verts, uint32_t n_verts, const uint32_t* indices, uint32_t n_indices,
+                   const uint8_t* tags, wt_mesh** out);
+void wt_mesh_destroy(wt_mesh* m);
+/* An rgba8unorm-srgb albedo texture, width x height RGBA8 texels from the top
+ * row; its mip chain is made with halveRgba (mesh-car.ts:30-44).  *index
+ * receives its number for wt_mesh_draw.texture. */
+int wt_mesh_add_texture(wt_mesh* m, uint32_t width, uint32_t height, const uint8_t* rgba, int32_t* index);
+/* Append a draw (record order = draw order; MeshCar sorts opaque before blended). */
+int wt_mesh_add_draw(wt_mesh* m, const wt_mesh_draw* d);
+/* The G-buffer pass (engine.ts:716): clear the G-buffer targets and the depth
+ * buffer, then the mesh's draws in order (the optional ones when optional != 0)
+ * with the camera and the Rig uniform (wt_set_car_model's rig).  Queued on the
+ * context's stream; a frame with decals waits once for their fragment count. */
+int wt_render_mesh(wt_renderer* r, wt_mesh* m, const wt_mesh_cam* cam, const wt_rig* rig, int optional);
+
+/* Reverse the PNG scanline filters (None, Sub, Up, Average, Paeth) of an
+ * inflated image: filtered holds rows x (1 + row_bytes) bytes (a filter-type
+ * byte, then the row), bpp the bytes per pixel (1 for bit depths below 8).
+ * out receives rows x row_bytes.  Host only; WT_ERR_ARG on an unknown filter.
+ * For decoding the mesh's textures (the browser's image decoder in the
+ * reference, main.ts:989-995). */
+int wt_png_unfilter(const uint8_t* filtered, uint32_t rows, uint32_t row_bytes, uint32_t bpp, uint8_t* out);
 
 int wt_info_get(wt_ctx* ctx, wt_info* out);
 

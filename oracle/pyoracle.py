@@ -80,6 +80,9 @@ def _load_ref():
     L.wtr_glow.argtypes = [_vp, _i, _i, _vp, _vp, ctypes.c_uint32, _vp, _vp, ctypes.c_uint32, _vp]
     L.wtr_scene_sdf.argtypes = [_vp, _vp, ctypes.c_uint32, _vp]
     L.wtr_set_car.argtypes = [_vp, _vp, _vp, _vp]
+    L.wtr_set_gbuffer.argtypes = [_i, _i, _vp, _vp, _vp]
+    L.wtr_mesh_gbuffer.argtypes = [_i, _i, _vp, ctypes.c_uint32, _vp, ctypes.c_uint32, _vp, _vp, _i, _i, _vp, _vp,
+                                   _vp, _vp, _vp, _vp, _vp, _vp]
     return L
 
 
@@ -99,6 +102,7 @@ def shade_model_lib():
         L.wthm_render.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _F, _vp, _vp] + [ctypes.c_uint32] * 4 + [_vp]
         L.wthm_scene_sdf.argtypes = [_vp, _vp, ctypes.c_uint32, _vp]
         L.wthm_set_car.argtypes = [_vp, _vp, _vp, _vp]
+        L.wthm_set_gbuffer.argtypes = [_vp, _vp, _vp]
         _S = L
     return _S
 
@@ -118,6 +122,24 @@ def shade_model_set_car(car):
             np.array(car.parts_dims, np.uint32), np.ascontiguousarray(car.rig, np.float32))
     L.wthm_set_car(*(a.ctypes.data for a in keep))
     _SCAR = keep
+
+
+_SGB = None
+
+
+def shade_model_set_gbuffer(albedo, normal, material):
+    """Bind the car G-buffer ([h, w, 4] float16, float16, uint8) to the host-built
+    shading code, or unbind it with None."""
+    global _SGB
+    L = shade_model_lib()
+    if albedo is None:
+        L.wthm_set_gbuffer(None, None, None)
+        _SGB = None
+        return
+    keep = (np.ascontiguousarray(albedo, np.float16).view(np.uint16), np.ascontiguousarray(normal, np.float16)
+            .view(np.uint16), np.ascontiguousarray(material, np.uint8))
+    L.wthm_set_gbuffer(*(a.ctypes.data for a in keep))
+    _SGB = keep
 
 
 def shade_model_render(shape, cam, look, view, dims, origin, h, fields, temps, width, height, threads=1, rows=None):
@@ -238,6 +260,52 @@ def ref_scene_sdf(shape, pts):
     out = np.zeros((p.shape[0], 2), np.float32)
     L.wtr_scene_sdf(w.ctypes.data, p.ctypes.data, p.shape[0], out.ctypes.data)
     return out
+
+
+_GB = None
+
+
+def ref_set_gbuffer(albedo, normal, material):
+    """Bind the car G-buffer ([h, w, 4] float16, float16, uint8, as the render
+    targets store them) to the translated RENDER shader, or unbind it with None."""
+    global _GB
+    L = ref_lib()
+    if albedo is None:
+        L.wtr_set_gbuffer(1, 1, None, None, None)
+        _GB = None
+        return
+    h, w = albedo.shape[:2]
+    keep = (np.ascontiguousarray(albedo, np.float16).astype(np.float32),
+            np.ascontiguousarray(normal, np.float16).astype(np.float32),
+            np.ascontiguousarray(material, np.uint8).astype(np.float32) / np.float32(255.0))
+    L.wtr_set_gbuffer(w, h, *(a.ctypes.data for a in keep))
+    _GB = keep
+
+
+def ref_mesh_gbuffer(data, cam, rig, width, height, gurney=False):
+    """The reference's MESH_DRAW shaders over a car mesh (windtunnel.mesh_car.MeshData)
+    in the restated WebGPU pipeline: the cleared G-buffer after the draws, as
+    (albedo [h, w, 4] float16, normal-distance float16, material uint8, depth float32)."""
+    from windtunnel.mesh_car import draw_words
+    L = ref_lib()
+    v = np.ascontiguousarray(data.verts, np.float32)
+    i = np.ascontiguousarray(data.indices, np.uint32)
+    t = np.zeros((data.tags.size + 3) // 4 * 4, np.uint8)
+    t[:data.tags.size] = data.tags
+    words = np.ascontiguousarray(draw_words(data, gurney))
+    texs = [np.ascontiguousarray(rgba, np.uint8) for (_, _, rgba) in data.textures]
+    dims = np.array([[w, h] for (w, h, _) in data.textures] or [[0, 0]], np.uint32)
+    ptrs = (ctypes.c_void_p * max(1, len(texs)))(*[a.ctypes.data for a in texs])
+    cw = np.frombuffer(bytes(cam), np.float32).copy()
+    r = np.ascontiguousarray(rig, np.float32)
+    albedo = np.zeros((height, width, 4), np.float32)
+    normal = np.zeros((height, width, 4), np.float32)
+    material = np.zeros((height, width, 4), np.uint8)
+    depth = np.ones((height, width), np.float32)
+    L.wtr_mesh_gbuffer(width, height, v.ctypes.data, v.shape[0], i.ctypes.data, i.size, t.ctypes.data,
+                       words.ctypes.data, words.shape[0], len(texs), dims.ctypes.data, ptrs, cw.ctypes.data,
+                       r.ctypes.data, albedo.ctypes.data, normal.ctypes.data, material.ctypes.data, depth.ctypes.data)
+    return albedo.astype(np.float16), normal.astype(np.float16), material, depth
 
 
 _CAR = None

@@ -13,6 +13,7 @@
 // in parallel on host threads.  Output of this file goes to oracle/_ref/.
 #include "wgsl_runtime.hpp"
 #include "_ref/wgsl_modules.inc"
+#include "../f1-wind-tunnel_gb300/csrc/wt_texfilter.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -388,6 +389,16 @@ void wtr_render_scene(const uint32_t* dims, const float* origin, float h, const 
   });
 }
 
+// The car G-buffer RENDER reads with look.meshMode != 0 (engine.ts:297-303):
+// w x h RGBA f32 texels holding the stored values (albedo and normal-distance
+// rounded to binary16, material c / 255).  NULL unbinds (textureLoad gives 0).
+void wtr_set_gbuffer(int w, int hgt, const float* albedo, const float* normal, const float* material) {
+  namespace M = m_render;
+  M::gAlbedo = rt::texture2d{w, hgt, albedo};
+  M::gNormal = rt::texture2d{w, hgt, normal};
+  M::gMaterial = rt::texture2d{w, hgt, material};
+}
+
 // The W17 model (engine.ts:410-421 setCarModel and the rig uniform of setShape):
 // sdf 368 x 84 x 67 binary16 (x fastest), parts pd[0] x pd[1] x pd[2] binary16,
 // rig the 87 vec4 of the Rig uniform (car-model.ts:60-69).  sdf == NULL clears it.
@@ -616,6 +627,271 @@ void wtr_glow(const float* scene, int w, int hgt, const float* parts, const uint
       }
   }
   for (size_t i = 0; i < acc.size(); i++) glow[i] = round_half((float)((double)acc[i] * 0x1p-32));
+}
+
+// ---- the car mesh G-buffer pass: MESH_DRAW (render-wgsl.ts:647-760) draws of
+// MeshCar.record (mesh-car.ts:205-207) into the cleared G-buffer (engine.ts:
+// 297-303, 716), run the way the WebGPU pipeline defines it: draws in order,
+// triangles in order, each fragment tested against the depth buffer as it is
+// at that moment.  Fixed-function stages:
+//   * triangle list of vertex_index 0..count-1 of each draw, cull none;
+//   * clipping to z >= 0 in clip space: the corners in order, a corner with
+//     z >= 0 kept, an edge whose ends lie on both sides adding the point at
+//     t = z_a / (z_a - z_b) with every output a + t (b - a); the polygon is drawn
+//     as the fan (0, 1, 2), (0, 2, 3); a part with a corner at w <= 0 is dropped;
+//   * viewport, coverage, tie rule, depth clip and perspective-correct
+//     varyings as in the glow pass above;
+//   * depth32float cleared to 1.  Opaque draws: 'less', depth written.  Blended
+//     draws (the decals): the bias depthBias * 2^(e - 23) + slopeScale * m with
+//     depthBias -4, slopeScale -1 (mesh-car.ts:150), e the exponent of the
+//     largest |z| of the part and m = max(|dz/dX|, |dz/dY|) from its plane, then
+//     clamped to [0, 1], 'less-equal', depth not written;
+//   * textureSample's derivatives: the uv differences across the fragment's
+//     2 x 2 pixel quad (from its top-left pixel to the right and down
+//     neighbours), the varyings there extrapolated from the same triangle;
+//     filtering as the texture filter header defines it;
+//   * targets: albedo and normalDist rgba16float, material rgba8unorm (the
+//     output rounding above).  Blended draws write albedo only, with
+//     DECAL_BLEND (mesh-car.ts:22-25): rgb = src.rgb * src.a + dst.rgb *
+//     (1 - src.a), alpha kept; the other targets have an empty write mask.
+extern "C++" {
+struct MVtx {
+  float X, Y, nz, iw;  // framebuffer position, NDC depth, 1 / clip w
+  float a[8];          // world xyz, normal xyz, uv
+};
+struct MeshTri {
+  MVtx v[3];
+  float A, sg, aa;
+  // barycentric weights (b) and perspective weights (w) at framebuffer point P
+  void edges(float Px, float Py, float* e) const {
+    e[0] = ((v[2].X - v[1].X) * (Py - v[1].Y) - (v[2].Y - v[1].Y) * (Px - v[1].X)) * sg;
+    e[1] = ((v[0].X - v[2].X) * (Py - v[2].Y) - (v[0].Y - v[2].Y) * (Px - v[2].X)) * sg;
+    e[2] = ((v[1].X - v[0].X) * (Py - v[0].Y) - (v[1].Y - v[0].Y) * (Px - v[0].X)) * sg;
+  }
+  void varyings(const float* e, float* out) const {
+    const float b0 = e[0] / aa, b1 = e[1] / aa, b2 = e[2] / aa;
+    const float q0 = b0 * v[0].iw, q1 = b1 * v[1].iw, q2 = b2 * v[2].iw;
+    const float qs = q0 + q1 + q2;
+    const float w0 = q0 / qs, w1 = q1 / qs, w2 = q2 / qs;
+    for (int k = 0; k < 8; k++) out[k] = w0 * v[0].a[k] + w1 * v[1].a[k] + w2 * v[2].a[k];
+  }
+};
+struct MeshTexture {
+  std::vector<std::vector<uint8_t>> data;
+  std::vector<wtx::Level> levels;
+};
+// halveRgba (mesh-car.ts:30-44)
+static std::vector<uint8_t> halve_rgba(const std::vector<uint8_t>& src, int w, int h, int* ow, int* oh) {
+  const int nw = std::max(1, w >> 1), nh = std::max(1, h >> 1);
+  std::vector<uint8_t> out((size_t)nw * nh * 4);
+  for (int y = 0; y < nh; y++) {
+    const int y0 = std::min(h - 1, y * 2), y1 = std::min(h - 1, y * 2 + 1);
+    for (int x = 0; x < nw; x++) {
+      const int x0 = std::min(w - 1, x * 2), x1 = std::min(w - 1, x * 2 + 1);
+      for (int c = 0; c < 4; c++)
+        out[((size_t)y * nw + x) * 4 + c] =
+            (uint8_t)((src[((size_t)y0 * w + x0) * 4 + c] + src[((size_t)y0 * w + x1) * 4 + c] +
+                       src[((size_t)y1 * w + x0) * 4 + c] + src[((size_t)y1 * w + x1) * 4 + c] + 2) >> 2);
+    }
+  }
+  *ow = nw;
+  *oh = nh;
+  return out;
+}
+static thread_local const MeshTexture* g_mesh_tex = nullptr;
+static thread_local float g_mesh_deriv[4];  // du/dx, dv/dx, du/dy, dv/dy of the current fragment
+static rt::vec4f mesh_sample(const rt::texture2d&, rt::vec2f uv) {
+  const wtx::Rgba c = wtx::sample(g_mesh_tex->levels.data(), (int)g_mesh_tex->levels.size(), uv.x, uv.y,
+                                  g_mesh_deriv[0], g_mesh_deriv[1], g_mesh_deriv[2], g_mesh_deriv[3]);
+  return rt::vec4f(c.r, c.g, c.b, c.a);
+}
+static MVtx mesh_vtx(const m_mesh::VOut& o, int W, int H) {
+  MVtx v;
+  const float nx = o.pos.x / o.pos.w, ny = o.pos.y / o.pos.w;
+  v.nz = o.pos.z / o.pos.w;
+  v.X = (nx * 0.5f + 0.5f) * (float)W;
+  v.Y = (0.5f - ny * 0.5f) * (float)H;
+  v.iw = 1.0f / o.pos.w;
+  const float a[8] = {o.world.x, o.world.y, o.world.z, o.normal.x, o.normal.y, o.normal.z, o.uv.x, o.uv.y};
+  for (int k = 0; k < 8; k++) v.a[k] = a[k];
+  return v;
+}
+static m_mesh::VOut vout_lerp(const m_mesh::VOut& a, const m_mesh::VOut& b, float t) {
+  auto l = [t](float x, float y) { return x + t * (y - x); };
+  m_mesh::VOut o{};
+  o.pos = rt::vec4f(l(a.pos.x, b.pos.x), l(a.pos.y, b.pos.y), l(a.pos.z, b.pos.z), l(a.pos.w, b.pos.w));
+  o.world = rt::vec3f(l(a.world.x, b.world.x), l(a.world.y, b.world.y), l(a.world.z, b.world.z));
+  o.normal = rt::vec3f(l(a.normal.x, b.normal.x), l(a.normal.y, b.normal.y), l(a.normal.z, b.normal.z));
+  o.uv = rt::vec2f(l(a.uv.x, b.uv.x), l(a.uv.y, b.uv.y));
+  return o;
+}
+// the part of triangle c[0..3) with z >= 0, as a polygon of 0, 3 or 4 corners
+static int clip_near(const m_mesh::VOut* c, m_mesh::VOut* out) {
+  int n = 0;
+  for (int i = 0; i < 3; i++) {
+    const m_mesh::VOut& a = c[i];
+    const m_mesh::VOut& b = c[(i + 1) % 3];
+    const bool ina = a.pos.z >= 0.0f, inb = b.pos.z >= 0.0f;
+    if (ina) out[n++] = a;
+    if (ina != inb) out[n++] = vout_lerp(a, b, a.pos.z / (a.pos.z - b.pos.z));
+  }
+  return n;
+}
+}  // extern "C++"
+
+// The G-buffer pass.  verts: nv x 8 floats (position, u, normal, v: the
+// vertex buffer of mesh-car.ts:63-77); indices[ni]; vparts: the part tags,
+// four per u32 (mesh-car.ts:88-91).  draws: nd records of 16 words in record
+// order: the MeshMat uniform (12 words: color, metal, rough, coat, alphaCut,
+// emissive, hasTex, isBody, firstIndex), vertex count, texture index (-1: none),
+// blend flag, unused.  textures: ntex level-0 RGBA8 images tex[i] of
+// tex_dims[2i] x tex_dims[2i+1]; their mip chains are made here.  cam: the
+// MeshCam uniform (24 words); rig: the 87 vec4 of the Rig uniform.  The targets
+// (w x h; albedo and normal as RGBA f32 holding binary16 values, material RGBA8,
+// depth f32) are read and written: the caller clears them.
+void wtr_mesh_gbuffer(int w, int hgt, const float* verts, uint32_t nv, const uint32_t* indices, uint32_t ni,
+                      const uint32_t* vparts, const uint32_t* draws, int nd, int ntex, const uint32_t* tex_dims,
+                      const uint8_t* const* tex, const float* cam, const float* rig, float* albedo, float* normal,
+                      uint8_t* material, float* depth) {
+  namespace M = m_mesh;
+  (void)nv;
+  (void)ni;
+  std::vector<MeshTexture> texs((size_t)std::max(ntex, 0));
+  for (int t = 0; t < ntex; t++) {
+    int tw = (int)tex_dims[2 * t], th = (int)tex_dims[2 * t + 1];
+    const int n_levels = (int)floor(log2((double)std::max(tw, th))) + 1;
+    texs[t].data.emplace_back(tex[t], tex[t] + (size_t)tw * th * 4);
+    std::vector<int> ws{tw}, hs{th};
+    for (int m = 1; m < n_levels; m++) {
+      int nw, nh;
+      texs[t].data.push_back(halve_rgba(texs[t].data.back(), ws.back(), hs.back(), &nw, &nh));
+      ws.push_back(nw);
+      hs.push_back(nh);
+    }
+    for (int m = 0; m < n_levels; m++) texs[t].levels.push_back(wtx::Level{texs[t].data[m].data(), ws[m], hs[m]});
+  }
+  float cf[24];
+  memcpy(cf, cam, sizeof(cf));
+  M::cam.viewProj = mat4(cf);
+  M::cam.camPos = v3(cf + 16); M::cam.rideH = cf[19];
+  M::cam.jitter = rt::vec2f(cf[20], cf[21]); M::cam.rake = cf[22]; M::cam.baseRide = cf[23];
+  {
+    auto v4 = [&](int i) { return rt::vec4f(rig[4 * i], rig[4 * i + 1], rig[4 * i + 2], rig[4 * i + 3]); };
+    for (int i = 0; i < 71; i++) M::rig.front[i] = v4(i);
+    M::rig.hinges = v4(71); M::rig.angles = v4(72); M::rig.extra = v4(73); M::rig.fly = v4(74);
+    for (int i = 0; i < 12; i++) M::rig.grids[i] = v4(75 + i);
+  }
+  M::verts.p = (rt::vec4f*)verts;
+  M::indices.p = (uint32_t*)indices;
+  M::vparts.p = (uint32_t*)vparts;
+  rt::sample_hook = mesh_sample;
+  for (int d = 0; d < nd; d++) {
+    const uint32_t* r = draws + 16 * d;
+    float f[12];
+    memcpy(f, r, sizeof(f));
+    M::mat.color = rt::vec4f(f[0], f[1], f[2], f[3]);
+    M::mat.metal = f[4]; M::mat.rough = f[5]; M::mat.coat = f[6]; M::mat.alphaCut = f[7];
+    M::mat.emissive = f[8]; M::mat.hasTex = f[9]; M::mat.isBody = f[10]; M::mat.firstIndex = r[11];
+    const uint32_t count = r[12];
+    const int texi = (int32_t)r[13];
+    const bool blend = r[14] != 0u;
+    g_mesh_tex = (texi >= 0 && texi < ntex) ? &texs[texi] : nullptr;
+    for (uint32_t t = 0; t + 2 < count; t += 3) {
+      M::VOut c[3], poly[4];
+      for (int k = 0; k < 3; k++) c[k] = M::vs_main(t + (uint32_t)k);
+      const int np = clip_near(c, poly);
+      for (int s = 0; s + 2 < np; s++) {
+        const M::VOut* tri[3] = {&poly[0], &poly[s + 1], &poly[s + 2]};
+        if (!(tri[0]->pos.w > 0.0f && tri[1]->pos.w > 0.0f && tri[2]->pos.w > 0.0f)) continue;
+        MeshTri T;
+        for (int k = 0; k < 3; k++) T.v[k] = mesh_vtx(*tri[k], w, hgt);
+        const MVtx* v = T.v;
+        T.A = (v[1].X - v[0].X) * (v[2].Y - v[0].Y) - (v[2].X - v[0].X) * (v[1].Y - v[0].Y);
+        if (!(T.A > 0.0f) && !(T.A < 0.0f)) continue;
+        T.sg = T.A > 0.0f ? 1.0f : -1.0f;
+        T.aa = T.A > 0.0f ? T.A : -T.A;
+        float bias = 0.0f;
+        if (blend) {
+          const float dzdx = ((v[1].nz - v[0].nz) * (v[2].Y - v[0].Y) - (v[2].nz - v[0].nz) * (v[1].Y - v[0].Y)) / T.A;
+          const float dzdy = ((v[2].nz - v[0].nz) * (v[1].X - v[0].X) - (v[1].nz - v[0].nz) * (v[2].X - v[0].X)) / T.A;
+          const float m = std::max(fabsf(dzdx), fabsf(dzdy));
+          const float zmax = std::max(fabsf(v[0].nz), std::max(fabsf(v[1].nz), fabsf(v[2].nz)));
+          int e = 0;
+          frexpf(zmax, &e);
+          bias = -4.0f * ldexpf(1.0f, e - 1 - 23) + -1.0f * m;
+        }
+        const float minx = std::min(v[0].X, std::min(v[1].X, v[2].X)), maxx = std::max(v[0].X, std::max(v[1].X, v[2].X));
+        const float miny = std::min(v[0].Y, std::min(v[1].Y, v[2].Y)), maxy = std::max(v[0].Y, std::max(v[1].Y, v[2].Y));
+        const int x0 = (int)ceilf(std::min(std::max(minx - 0.5f, 0.0f), (float)w));
+        const int x1 = (int)floorf(std::max(std::min(maxx - 0.5f, (float)(w - 1)), -1.0f));
+        const int y0 = (int)ceilf(std::min(std::max(miny - 0.5f, 0.0f), (float)hgt));
+        const int y1 = (int)floorf(std::max(std::min(maxy - 0.5f, (float)(hgt - 1)), -1.0f));
+        const bool own0 = raster_edge_owned((v[2].X - v[1].X) * T.sg, (v[2].Y - v[1].Y) * T.sg);
+        const bool own1 = raster_edge_owned((v[0].X - v[2].X) * T.sg, (v[0].Y - v[2].Y) * T.sg);
+        const bool own2 = raster_edge_owned((v[1].X - v[0].X) * T.sg, (v[1].Y - v[0].Y) * T.sg);
+        for (int py = y0; py <= y1; py++)
+          for (int px = x0; px <= x1; px++) {
+            const float Px = (float)px + 0.5f, Py = (float)py + 0.5f;
+            float e[3];
+            T.edges(Px, Py, e);
+            if (e[0] < 0.0f || e[1] < 0.0f || e[2] < 0.0f) continue;
+            if ((e[0] == 0.0f && !own0) || (e[1] == 0.0f && !own1) || (e[2] == 0.0f && !own2)) continue;
+            const float b0 = e[0] / T.aa, b1 = e[1] / T.aa, b2 = e[2] / T.aa;
+            const float z = b0 * v[0].nz + b1 * v[1].nz + b2 * v[2].nz;
+            if (!(z >= 0.0f && z <= 1.0f)) continue;
+            const size_t pi = (size_t)py * w + px;
+            if (blend) {
+              float zb = z + bias;
+              zb = zb < 0.0f ? 0.0f : (zb > 1.0f ? 1.0f : zb);
+              if (!(zb <= depth[pi])) continue;
+            } else if (!(z < depth[pi])) {
+              continue;
+            }
+            float a[8];
+            T.varyings(e, a);
+            if (g_mesh_tex) {
+              const float qx = (float)(px & ~1) + 0.5f, qy = (float)(py & ~1) + 0.5f;
+              float e00[3], e10[3], e01[3], a00[8], a10[8], a01[8];
+              T.edges(qx, qy, e00);
+              T.edges(qx + 1.0f, qy, e10);
+              T.edges(qx, qy + 1.0f, e01);
+              T.varyings(e00, a00);
+              T.varyings(e10, a10);
+              T.varyings(e01, a01);
+              g_mesh_deriv[0] = a10[6] - a00[6]; g_mesh_deriv[1] = a10[7] - a00[7];
+              g_mesh_deriv[2] = a01[6] - a00[6]; g_mesh_deriv[3] = a01[7] - a00[7];
+            }
+            M::VOut in{};
+            in.pos = rt::vec4f(Px, Py, z, 1.0f);
+            in.world = rt::vec3f(a[0], a[1], a[2]);
+            in.normal = rt::vec3f(a[3], a[4], a[5]);
+            in.uv = rt::vec2f(a[6], a[7]);
+            M::rt_discarded = false;
+            const M::GOut g = M::fs_main(in);
+            if (M::rt_discarded) continue;
+            float* al = albedo + pi * 4;
+            if (blend) {
+              const float sa = g.albedo.w;
+              al[0] = round_half(g.albedo.x * sa + al[0] * (1.0f - sa));
+              al[1] = round_half(g.albedo.y * sa + al[1] * (1.0f - sa));
+              al[2] = round_half(g.albedo.z * sa + al[2] * (1.0f - sa));
+              continue;
+            }
+            al[0] = round_half(g.albedo.x); al[1] = round_half(g.albedo.y);
+            al[2] = round_half(g.albedo.z); al[3] = round_half(g.albedo.w);
+            float* nd4 = normal + pi * 4;
+            nd4[0] = round_half(g.normalDist.x); nd4[1] = round_half(g.normalDist.y);
+            nd4[2] = round_half(g.normalDist.z); nd4[3] = round_half(g.normalDist.w);
+            uint8_t* m8 = material + pi * 4;
+            m8[0] = unorm8(g.material.x); m8[1] = unorm8(g.material.y);
+            m8[2] = unorm8(g.material.z); m8[3] = unorm8(g.material.w);
+            depth[pi] = z;
+          }
+      }
+    }
+  }
+  rt::sample_hook = nullptr;
+  g_mesh_tex = nullptr;
 }
 
 int wtr_threads(void) {

@@ -59,6 +59,17 @@ void wthm_set_car(const uint16_t* body, const uint16_t* parts, const uint32_t* p
   g_car.rig = g_rig.data();
 }
 
+// The car G-buffer of the mesh pass, w x h texels (binary16 albedo and
+// normal-distance, RGBA8 material) read when look.mesh_mode != 0; NULL unbinds.
+static const uint16_t* g_gb_albedo = nullptr;
+static const uint16_t* g_gb_normal = nullptr;
+static const uint8_t* g_gb_material = nullptr;
+void wthm_set_gbuffer(const uint16_t* albedo, const uint16_t* normal, const uint8_t* material) {
+  g_gb_albedo = albedo;
+  g_gb_normal = normal;
+  g_gb_material = material;
+}
+
 // RENDER fs_main over rows [y0, y1) of a w x h target: out[(y*w + x)*4 + k] =
 // colour, hit distance (rows outside the range untouched).  shape: wt_shape;
 // cam/look/view: the wt_cam / wt_look / wt_view structs; fields (n x 4) and
@@ -94,6 +105,11 @@ void wthm_render(const void* shape, const void* cam_p, const void* look_p, const
   a.surf_mode = look.surf_mode; a.palette = look.palette; a.carbon_body = look.carbon_body; a.is_f1 = look.is_f1;
   a.slice_axis = look.slice_axis; a.show_flow = look.show_flow; a.slice_pos = look.slice_pos;
   a.slice_alpha = look.slice_alpha;
+  a.mesh_mode = look.mesh_mode; a.cooling = look.cooling;
+  a.g_albedo = reinterpret_cast<const ushort4*>(g_gb_albedo);
+  a.g_normal = reinterpret_cast<const ushort4*>(g_gb_normal);
+  a.g_material = reinterpret_cast<const uchar4*>(g_gb_material);
+  if (a.mesh_mode != 0u && !(g_gb_albedo && g_gb_normal && g_gb_material)) return;
   a.key = f3n(-0.32f, 0.90f, 0.30f);
   a.fill_a = f3n(0.6f, 0.35f, -0.7f);
   a.fill_b = f3n(0.6f, 0.35f, 0.7f);

@@ -110,6 +110,8 @@ template <class T> struct vec4 {
   template <class S, class C, class D>
   vec4(const vec2<S>& v, C c, D d) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(c)), w(cv<T>(d)) {}
   template <class S> vec4(const vec4<S>& v) : x(cv<T>(v.x)), y(cv<T>(v.y)), z(cv<T>(v.z)), w(cv<T>(v.w)) {}
+  template <class S, class R>
+  vec4(const vec2<S>& a, const vec2<R>& b) : x(cv<T>(a.x)), y(cv<T>(a.y)), z(cv<T>(b.x)), w(cv<T>(b.y)) {}
   vec4(const vec4& v) = default;
   vec4& operator=(const vec4& v) = default;
   vec2<T> xy() const { return vec2<T>(x, y); }
@@ -244,6 +246,11 @@ struct texture2d {
   const f32* p = nullptr;
 };
 static inline vec2u textureDimensions(const texture2d& t) { return vec2u((u32)t.w, (u32)t.h); }
+// textureSample (implicit level of detail) is the rasterizer's: the driver that
+// runs a fragment shader installs a hook that knows the fragment's derivatives.
+typedef vec4f (*sample_hook_fn)(const texture2d&, vec2f);
+inline thread_local sample_hook_fn sample_hook = nullptr;
+static inline vec4f textureSample(const texture2d& t, const sampler&, vec2f uv) { return sample_hook(t, uv); }
 static inline vec4f textureLoad(const texture2d& t, vec2i q, i32) {
   if (!t.p || q.x < 0 || q.y < 0 || q.x >= t.w || q.y >= t.h) return vec4f(0.0f);
   const f32* e = t.p + ((size_t)q.y * (size_t)t.w + (size_t)q.x) * 4;
@@ -332,4 +339,4 @@ template <class T> static inline T atomicLoad(T* p) { return __atomic_load_n(p, 
   using rt::atomicLoad; using rt::textureSampleLevel; using rt::textureDimensions;                 \
   using rt::texture2d; using rt::textureLoad; using rt::mat4x4f; using rt::all; using rt::atan2;    \
   using rt::exp; using rt::exp2; using rt::log2; using rt::pow; using rt::fract; using rt::step;     \
-  using rt::reflect; using rt::distance;
+  using rt::reflect; using rt::distance; using rt::textureSample;

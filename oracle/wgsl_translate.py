@@ -206,6 +206,8 @@ def cxx_type(t):
         return "texture3d"
     if t == "texture_2d<f32>":
         return "texture2d"
+    if t == "sampler":
+        return "sampler"
     return t
 
 
@@ -454,6 +456,7 @@ def main():
         "m_taa": "TAA",
         "m_pdraw": "PARTICLES_DRAW",
         "m_sdraw": "STREAM_DRAW",
+        "m_mesh": "MESH_DRAW",
     }
     os.makedirs(OUT, exist_ok=True)
     chunks = [

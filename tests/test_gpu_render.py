@@ -95,12 +95,15 @@ def test_render_errors(setup):
     lk_mesh = type(lk).from_buffer_copy(lk)
     lk_mesh.mesh_mode = 1
     u = R.FrameState().next(f["cam"], (16, 8))
-    with pytest.raises(WindTunnelError, match="mesh_mode"):
-        r.scene(u.cam, lk_mesh, mc.view())
+    # meshMode over the cleared G-buffer: no car texels, so only ground and backdrop
+    r.scene(u.cam, lk_mesh, mc.view())
+    assert (r.read(R.TARGET_GNORMAL) == 0).all()
     with pytest.raises(WindTunnelError, match="cur"):
         r.taa(u.taa, 2)
     with pytest.raises(WindTunnelError, match="unknown target"):
-        e._check(e.lib.wt_render_read(r.r, 9, np.zeros(4).ctypes.data), "wt_render_read")
+        e._check(e.lib.wt_render_read(r.r, 10, np.zeros(4).ctypes.data), "wt_render_read")
+    with pytest.raises(WindTunnelError, match="mesh missing"):
+        e._check(e.lib.wt_render_mesh(r.r, None, None, None, 0), "wt_render_mesh")
     r.scene(u.cam, lk, mc.view())  # the renderer stays usable
     r.close()
 
