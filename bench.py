@@ -281,6 +281,9 @@ def run_surrogate(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+MESH_DETAIL = 2.8  # stand-in mesh tessellation: about the W17 mesh's 268k triangles
+
+
 def run_render(args, rank, world):
     """The render passes of the headless check's hero frame at 1280x720 (scene
     ray march, TAA, streamline glow, bloom, present) over a developed flow of
@@ -294,9 +297,20 @@ def run_render(args, rank, world):
     from windtunnel.render import FrameState, make_look
     from windtunnel.viewer import HEADLESS_SHAPE, Viewer, orbit
     W, H = 1280, 720
+    w17 = args.workload == "render-w17"
     eng = AeroEngine("medium")
     viewer = Viewer(eng, W, H, particles=1)
-    eng.set_shape(HEADLESS_SHAPE)
+    shape_p = HEADLESS_SHAPE
+    mesh = None
+    if w17:
+        from windtunnel.car_model import synthetic_w17
+        from windtunnel.mesh_car import MeshCar, synthetic_mesh
+        from windtunnel.viewer import W17_SHAPE
+        shape_p = W17_SHAPE
+        eng.set_car_model(synthetic_w17(shape_p))
+        mesh = MeshCar(eng, synthetic_mesh(MESH_DETAIL))
+        viewer.set_mesh(mesh)
+    eng.set_shape(shape_p)
     eng.reset()
     cam = orbit({}, W / H)
     for _ in range(40):                       # develop the flow
@@ -304,12 +318,13 @@ def run_render(args, rank, world):
     view = viewer.view_uniform()
     sp = viewer.stream_params()
     lines = eng.streamlines(sp, view)
-    look = make_look(HEADLESS_SHAPE)
+    look = make_look(shape_p)
     r = viewer.renderer
     stream = torch.cuda.ExternalStream(eng.stream())
+    mesh_args = dict(mesh=mesh, rig=eng.car_model.rig, params=shape_p) if w17 else {}
 
     def passes():
-        r.frame(cam, look, view, lines=lines, flow_time=0.5)
+        r.frame(cam, look, view, lines=lines, flow_time=0.5, **mesh_args)
 
     for _ in range(max(3, args.warmup)):
         passes()
@@ -323,12 +338,26 @@ def run_render(args, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
-    # the scene pass alone (the dominant kernel)
+    # the scene pass alone (the dominant kernel), and the mesh pass alone
     u = FrameState().next(cam, (W, H), lines=lines)
+    look_s = look
+    mesh_ms = None
+    if w17:
+        from windtunnel.mesh_car import mesh_cam
+        mcam = mesh_cam(cam, (W, H), u.halton, shape_p)
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        for _ in range(steps):
+            r.mesh(mesh, mcam, eng.car_model.rig)
+        m1.record(stream)
+        torch.cuda.synchronize()
+        mesh_ms = m0.elapsed_time(m1) / steps
+        look_s = type(look).from_buffer_copy(look)
+        look_s.mesh_mode = 1
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s0.record(stream)
     for _ in range(steps):
-        r.scene(u.cam, look, view)
+        r.scene(u.cam, look_s, view)
     s1.record(stream)
     torch.cuda.synchronize()
     scene_ms = s0.elapsed_time(s1) / steps
@@ -341,7 +370,7 @@ def run_render(args, rank, world):
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_frames
     line_bytes = sp.lines * sp.steps * 16
     base = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not w17:
         # the render passes' dominant part, the scene pass, in the device code built
         # for the host, on all host cores: a band of rows, scaled to the full frame
         from windtunnel.engine import pack_shape
@@ -363,20 +392,29 @@ def run_render(args, rank, world):
             "metric": "render_ms_per_frame", "value": ms, "unit": "ms", "n_gpus": world, "steps": steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "headless-check hero frame at 1280x720: scene ray march of the generic F1, TAA, "
-                                   "streamline glow (90 lines x 360 points), bloom, present; medium lattice "
-                                   "232x68x52 after 40 frames",
-                       "image": [W, H], "scene_pass_ms": scene_ms,
+            "config": {"workload": (
+                           "headless-check hero frame at 1280x720 of the W17 scene drawn from its mesh: G-buffer "
+                           f"pass of the stand-in mesh ({mesh.data.indices.size // 3} triangles, textured, 2 decal "
+                           "draws), scene composite with ground reflection march, TAA, streamline glow (90 lines x "
+                           "360 points), bloom, present; medium lattice 232x68x52 after 40 frames") if w17 else (
+                           "headless-check hero frame at 1280x720: scene ray march of the generic F1, TAA, "
+                           "streamline glow (90 lines x 360 points), bloom, present; medium lattice "
+                           "232x68x52 after 40 frames"),
+                       "image": [W, H], "scene_pass_ms": scene_ms, "mesh_pass_ms": mesh_ms,
                        "l2": "targets (29 MB) fit L2: the passes are compute-bound, no flush"},
             "roofline": None,
             "roofline_note": "scene pass: ALU / instruction-issue bound ray march, not HBM or tensor; "
                              "issue utilisation in profiles/render_scene_f1_1280x720.md",
             "cpu_baseline": base,
+            "cpu_baseline_note": ("the mesh pass's CPU form is the oracle's pipeline around the reference's "
+                                  "translated shaders, built only where the reference checkout is") if w17 else None,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": line_bytes + 4 * 24 * 4,
                     "d2h_bytes_per_step": line_bytes + W * H * 4},
-            "gpu_launches": steps * 7,
+            "gpu_launches": steps * (7 + (14 if w17 else 0)),
             "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
         }), flush=True)
+    if mesh is not None:
+        mesh.close()
     viewer.close()
     eng.close()
 
@@ -387,7 +425,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200, help="timed frames")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="wt", choices=["wt", "reference"])
-    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "surrogate", "render"])
+    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "surrogate", "render",
+                                                              "render-w17"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-frames", type=int, default=64, help="CPU-baseline frames (stops at 20 s)")
@@ -431,7 +470,7 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    if args.workload == "render":
+    if args.workload in ("render", "render-w17"):
         run_render(args, rank, world)
         if dist:
             dist.destroy_process_group()

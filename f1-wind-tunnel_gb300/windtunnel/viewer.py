@@ -11,6 +11,7 @@ render passes into a headless RGBA8 image, plus the headless check
     write_png("hero.png", v.image())
 
     python -m windtunnel.viewer --frames 240 --out shots/     # the headless check
+    python -m windtunnel.viewer --w17 --out shots/            # the W17 car, mesh-drawn (stand-in assets)
 
 Particles live in host memory and go through wt_particles_step each frame;
 streamlines through wt_streamlines; everything else stays on the device.
@@ -93,6 +94,7 @@ class Viewer:
         self.scatter_frames = 2
         self.flow_time = 0.0
         self.view = ViewParams()
+        self.mesh = None   # the car mesh the W17 scene draws into the G-buffer (engine.ts:679)
 
     def _quality(self):
         for q, d in QUALITIES.items():
@@ -105,6 +107,10 @@ class Viewer:
 
     def set_view(self, v: ViewParams):
         self.view = v
+
+    def set_mesh(self, mesh):
+        """A mesh_car.MeshCar for the W17 scene (setCarModel's mesh, engine.ts:410-421)."""
+        self.mesh = mesh
 
     def reset_particles(self):
         """reset() restarts the particles with two scatter frames (engine.ts:380)."""
@@ -202,8 +208,12 @@ class Viewer:
                          slice_axis=v.slice_axis, slice_pos=v.slice_pos, paint=v.livery.paint,
                          accent=v.livery.accent, carbon=v.livery.carbon,
                          cooling=e.shape_params.cooling if e.shape_params is not None else 1)
+        p = e.shape_params
+        mesh_mode = (self.mesh is not None and p is not None and p.kind == ShapeKind.W17 and
+                     getattr(e, "car_model", None) is not None)
         self.renderer.frame(cam, look, view, dt, v.kmh, parts, color_mode, v.flow_mode == FlowMode.Smoke, lines,
-                            self.flow_time, v.flow_mode == FlowMode.Vortices)
+                            self.flow_time, v.flow_mode == FlowMode.Vortices, mesh=self.mesh if mesh_mode else None,
+                            rig=e.car_model.rig if mesh_mode else None, params=p)
 
     def image(self):
         return self.renderer.read(TARGET_OUTPUT)
@@ -231,14 +241,27 @@ def orbit(o, aspect):
     return orbit_camera(d["target"], d["yaw"], d["pitch"], d["distance"], aspect)
 
 
-def headless_check(quality="medium", frames=240, out_dir=None, only=None, width=1280, height=720):
+W17_SHAPE = ShapeParams(kind=ShapeKind.W17, rideH=0.12, rearRideH=0.14)   # wing-sensitivity.ts's W17 setup
+
+
+def headless_check(quality="medium", frames=240, out_dir=None, only=None, width=1280, height=720, w17=False,
+                   assets=None):
     """scripts/headless-check.ts: run `frames` frames of 8 steps, print the
-    summary line, then render the shots (6 frames of 2 steps each) to PNG."""
+    summary line, then render the shots (6 frames of 2 steps each) to PNG.
+    With w17 the car is the baked W17 model drawn from its mesh (the reference's
+    assets from `assets`, else the stand-ins of car_model and mesh_car)."""
     engine = AeroEngine(quality)
     viewer = Viewer(engine, width, height)
     base = ViewParams()
     viewer.set_view(base)
-    engine.set_shape(HEADLESS_SHAPE)
+    mesh = None
+    if w17:
+        from .car_model import load_w17, synthetic_w17
+        from .mesh_car import MeshCar, load_w17_mesh, synthetic_mesh
+        engine.set_car_model(load_w17(assets, W17_SHAPE) if assets else synthetic_w17(W17_SHAPE))
+        mesh = MeshCar(engine, load_w17_mesh(assets) if assets else synthetic_mesh())
+        viewer.set_mesh(mesh)
+    engine.set_shape(W17_SHAPE if w17 else HEADLESS_SHAPE)
     engine.reset()
     viewer.reset_particles()
     aspect = width / height
@@ -271,6 +294,8 @@ def headless_check(quality="medium", frames=240, out_dir=None, only=None, width=
             path = os.path.join(out_dir, f"{name}.png")
             write_png(path, viewer.image())
             written.append(path)
+    if mesh is not None:
+        mesh.close()
     viewer.close()
     engine.close()
     return summary, written
@@ -283,9 +308,11 @@ def main(argv=None):
     ap.add_argument("--out", default=None, help="directory for the PNG shots")
     ap.add_argument("--only", default=None)
     ap.add_argument("--size", default="1280x720")
+    ap.add_argument("--w17", action="store_true", help="the baked W17 car, drawn from its mesh")
+    ap.add_argument("--assets", default=None, help="the reference's public/models directory (W17 assets)")
     a = ap.parse_args(argv)
     w, h = (int(x) for x in a.size.split("x"))
-    headless_check(a.quality, a.frames, a.out, a.only, w, h)
+    headless_check(a.quality, a.frames, a.out, a.only, w, h, a.w17, a.assets)
 
 
 if __name__ == "__main__":
