@@ -1310,7 +1310,7 @@ struct wt_renderer {
   uint32_t* m_dcount = nullptr;
   uint32_t* m_doff = nullptr;
   uint32_t* m_dcur = nullptr;
-  uint32_t* m_nbig = nullptr;
+  unsigned long long* m_nbig = nullptr;
   uint32_t* m_dslots = nullptr;
   size_t m_slots_cap = 0;
   float4* m_corners = nullptr;
@@ -1357,7 +1357,8 @@ void release_renderer_buffers(wt_renderer* r) {
     if (b) cudaFree(b);
   r->m_depth = nullptr;
   r->m_keys = nullptr;
-  r->m_dcount = r->m_doff = r->m_dcur = r->m_nbig = r->m_dslots = nullptr;
+  r->m_dcount = r->m_doff = r->m_dcur = r->m_dslots = nullptr;
+  r->m_nbig = nullptr;
   r->m_corners = nullptr;
   r->m_big = nullptr;
   r->m_scan = nullptr;
@@ -1852,7 +1853,7 @@ int wt_render_mesh(wt_renderer* r, wt_mesh* m, const wt_mesh_cam* cam, const wt_
     WT_CUDA(c, cudaMalloc((void**)&r->m_dcount, px * 4));
     WT_CUDA(c, cudaMalloc((void**)&r->m_doff, px * 4));
     WT_CUDA(c, cudaMalloc((void**)&r->m_dcur, px * 4));
-    WT_CUDA(c, cudaMalloc((void**)&r->m_nbig, 4));
+    WT_CUDA(c, cudaMalloc((void**)&r->m_nbig, 8));
   }
   WT_CUDA(c, grow(&r->m_corners, &r->m_corners_cap, (size_t)corners * 3));
   WT_CUDA(c, grow(&r->m_big, &r->m_big_cap, (size_t)tris * 2));
@@ -1875,7 +1876,7 @@ int wt_render_mesh(wt_renderer* r, wt_mesh* m, const wt_mesh_cam* cam, const wt_
   a.w = r->w; a.h = r->h;
   a.corners = r->m_corners;
   a.depth = r->m_depth; a.keys = r->m_keys;
-  a.big = r->m_big; a.n_big = r->m_nbig; a.big_cap = (uint32_t)std::min<size_t>(r->m_big_cap, 0xffffffffu);
+  a.big = r->m_big; a.big_count = r->m_nbig; a.big_cap = (uint32_t)std::min<size_t>(r->m_big_cap, 0xffffffffu);
   a.g_albedo = r->g_albedo; a.g_normal = r->g_normal; a.g_material = r->g_material;
   a.dcount = r->m_dcount; a.doff = r->m_doff; a.dcur = r->m_dcur; a.dslots = r->m_dslots;
   WT_CUDA(c, launch_mesh_clear(a, c->stream));

@@ -40,7 +40,8 @@ namespace wt {
 namespace {
 
 constexpr uint32_t KEEP = 0xffffffffu;  // visibility key: the pixel keeps its earlier fragment
-constexpr int BIG_PIXELS = 1024;        // bounding boxes above this go to a block per triangle
+constexpr int BIG_PIXELS = 1024;        // bounding boxes above this are split into tiles
+constexpr int TILE = 32;                // pixels per side of a tile of a large triangle
 
 struct Corner {
   float4 pos;
@@ -324,13 +325,14 @@ __device__ __forceinline__ unsigned long long vis_key(float z, uint32_t seq) {
 }
 
 // ---------------------------------------------------------------- rasterization
-// Every pixel of T's bounding box, strided over `lanes` threads.
+// Every pixel of the rectangle [x0, x1] x [y0, y1] (within T's bounding box),
+// strided over `lanes` threads.
 template <class Op>
-__device__ void raster(const Tri& T, int lane, int lanes, Op op) {
-  const int bw = T.x1 - T.x0 + 1;
-  const int n = bw * (T.y1 - T.y0 + 1);
+__device__ void raster(const Tri& T, int x0, int x1, int y0, int y1, int lane, int lanes, Op op) {
+  const int bw = x1 - x0 + 1;
+  const int n = bw * (y1 - y0 + 1);
   for (int i = lane; i < n; i += lanes) {
-    const int px = T.x0 + i % bw, py = T.y0 + i / bw;
+    const int px = x0 + i % bw, py = y0 + i / bw;
     float e[3];
     T.edges((float)px + 0.5f, (float)py + 0.5f, e);
     if (!T.covers(e)) continue;
@@ -372,14 +374,19 @@ struct DecalOp {
 
 // kind 0: opaque visibility, 1: decal count, 2: decal fill
 template <int KIND>
-__device__ void raster_part(const MeshArgs& a, const MeshDraw& d, const Tri& T, uint32_t tri, int s, int lane,
-                            int lanes) {
+__device__ void raster_part(const MeshArgs& a, const MeshDraw& d, const Tri& T, uint32_t tri, int s, int x0, int x1,
+                            int y0, int y1, int lane, int lanes) {
   const uint32_t seq = tri * 2u + (uint32_t)s;
-  if (KIND == 0) raster(T, lane, lanes, OpaqueOp{&a, &d, &T, seq});
-  else raster(T, lane, lanes, DecalOp{&a, &T, seq, KIND == 2});
+  if (KIND == 0) raster(T, x0, x1, y0, y1, lane, lanes, OpaqueOp{&a, &d, &T, seq});
+  else raster(T, x0, x1, y0, y1, lane, lanes, DecalOp{&a, &T, seq, KIND == 2});
 }
+__device__ __forceinline__ uint32_t tiles_x(const Tri& T) { return (uint32_t)(T.x1 - T.x0 + TILE) / TILE; }
+__device__ __forceinline__ uint32_t tiles_y(const Tri& T) { return (uint32_t)(T.y1 - T.y0 + TILE) / TILE; }
 
-// One thread per triangle of draws [d0, d1); large footprints are deferred.
+// One thread per triangle of draws [d0, d1).  A large footprint is deferred as
+// TILE x TILE tiles: one 64-bit atomic gives the part its list slot (high word)
+// and the sequence number of its first tile (low word), so the list is ordered
+// by first tile and a tile finds its part by binary search.
 template <int KIND>
 __global__ void mesh_raster_kernel(const MeshArgs a, uint32_t d0, uint32_t d1, uint32_t tri0, uint32_t tri1) {
   const uint32_t tri = tri0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -389,24 +396,34 @@ __global__ void mesh_raster_kernel(const MeshArgs a, uint32_t d0, uint32_t d1, u
     Tri T;
     if (!setup_tri(a, d, tri - d.tri_base, s, T)) continue;
     if ((T.x1 - T.x0 + 1) * (T.y1 - T.y0 + 1) > BIG_PIXELS) {
-      const uint32_t slot = atomicAdd(a.n_big, 1u);
-      if (slot < a.big_cap) a.big[slot] = make_uint4(tri, (uint32_t)s, 0u, 0u);
+      const unsigned long long old = atomicAdd(a.big_count, (1ull << 32) | (tiles_x(T) * tiles_y(T)));
+      const uint32_t slot = (uint32_t)(old >> 32);
+      if (slot < a.big_cap) a.big[slot] = make_uint4(tri, (uint32_t)s, (uint32_t)old, 0u);  // never full: 2 per triangle
       continue;
     }
-    raster_part<KIND>(a, d, T, tri, s, 0, 1);
+    raster_part<KIND>(a, d, T, tri, s, T.x0, T.x1, T.y0, T.y1, 0, 1);
   }
 }
 
-// The deferred large triangles, a block each (grid-strided over the list).
+// The tiles of the deferred large triangles, a block each (grid-strided).
 template <int KIND>
 __global__ void mesh_raster_big_kernel(const MeshArgs a, uint32_t d0, uint32_t d1) {
-  const uint32_t n = min(*a.n_big, a.big_cap);
-  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-    const uint4 b = a.big[i];
+  const unsigned long long count = *a.big_count;
+  const uint32_t n = min((uint32_t)(count >> 32), a.big_cap), tiles = (uint32_t)count;
+  for (uint32_t u = blockIdx.x; u < tiles; u += gridDim.x) {
+    uint32_t lo = 0, hi = n;  // the last part whose first tile is <= u
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) / 2;
+      if (a.big[mid].z <= u) lo = mid; else hi = mid;
+    }
+    const uint4 b = a.big[lo];
     const MeshDraw& d = a.draws[find_draw(a, d0, d1, b.x)];
     Tri T;
     if (!setup_tri(a, d, b.x - d.tri_base, (int)b.y, T)) continue;
-    raster_part<KIND>(a, d, T, b.x, (int)b.y, threadIdx.x, blockDim.x);
+    const uint32_t t = u - b.z, tx = tiles_x(T);
+    const int x0 = T.x0 + (int)(t % tx) * TILE, y0 = T.y0 + (int)(t / tx) * TILE;
+    raster_part<KIND>(a, d, T, b.x, (int)b.y, x0, min(x0 + TILE - 1, T.x1), y0, min(y0 + TILE - 1, T.y1),
+                      threadIdx.x, blockDim.x);
   }
 }
 
@@ -499,7 +516,7 @@ cudaError_t launch_mesh_vertex(const MeshArgs& a, uint32_t corners, cudaStream_t
 namespace {
 template <int KIND>
 cudaError_t raster_draws(const MeshArgs& a, uint32_t d0, uint32_t d1, uint32_t tri0, uint32_t tri1, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(a.n_big, 0, sizeof(uint32_t), s);
+  cudaError_t e = cudaMemsetAsync(a.big_count, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   if (tri1 <= tri0) return cudaSuccess;
   mesh_raster_kernel<KIND><<<(tri1 - tri0 + 127) / 128, 128, 0, s>>>(a, d0, d1, tri0, tri1);

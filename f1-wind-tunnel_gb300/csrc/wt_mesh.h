@@ -45,8 +45,8 @@ struct MeshArgs {
   float4* corners;          // vertex shader outputs: 3 float4 per corner
   float* depth;             // depth32float
   unsigned long long* keys; // visibility: depth bits << 32 | triangle sequence * 2 + part
-  uint4* big;               // triangles with a large footprint, deferred to a block each
-  uint32_t* n_big;
+  uint4* big;               // parts with a large footprint: (triangle, part, first tile, 0)
+  unsigned long long* big_count;  // parts << 32 | tiles
   uint32_t big_cap;
   ushort4* g_albedo;
   ushort4* g_normal;
