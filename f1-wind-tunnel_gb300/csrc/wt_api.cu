@@ -1874,7 +1874,8 @@ int wt_render_mesh(wt_renderer* r, wt_mesh* m, const wt_mesh_cam* cam, const wt_
   WT_CUDA(c, cudaMemcpyAsync(r->m_rig, rig, sizeof(wt_rig), cudaMemcpyHostToDevice, c->stream));
   a.rig = r->m_rig;
   a.w = r->w; a.h = r->h;
-  a.corners = r->m_corners;
+  a.cpos = r->m_corners;
+  a.cattr = r->m_corners + corners;
   a.depth = r->m_depth; a.keys = r->m_keys;
   a.big = r->m_big; a.big_count = r->m_nbig; a.big_cap = (uint32_t)std::min<size_t>(r->m_big_cap, 0xffffffffu);
   a.g_albedo = r->g_albedo; a.g_normal = r->g_normal; a.g_material = r->g_material;

@@ -43,10 +43,15 @@ constexpr uint32_t KEEP = 0xffffffffu;  // visibility key: the pixel keeps its e
 constexpr int BIG_PIXELS = 1024;        // bounding boxes above this are split into tiles
 constexpr int TILE = 32;                // pixels per side of a tile of a large triangle
 
-struct Corner {
+// A corner after the vertex shader: position and, when ATTR, the varyings
+// (world xyz, normal xyz, uv).  Coverage and depth need the position only.
+template <bool ATTR>
+struct CornerT {
   float4 pos;
-  float a[8];  // world xyz, normal xyz, uv
+  float a[ATTR ? 8 : 1];
 };
+using Corner = CornerT<true>;
+constexpr int nattr(bool attr) { return attr ? 8 : 0; }
 
 // ---------------------------------------------------------------- vertex stage
 // rigRotate with dir = +1, rigRotateDir and podDeform with dir = +1
@@ -144,37 +149,41 @@ __global__ void mesh_vertex_kernel(const MeshArgs a, uint32_t corners) {
   }
   const MeshDraw& d = a.draws[lo];
   const Corner o = mesh_vs(a, d, c - d.corner_base);
-  float4* out = a.corners + 3 * (size_t)c;
-  out[0] = o.pos;
-  out[1] = make_float4(o.a[0], o.a[1], o.a[2], o.a[6]);
-  out[2] = make_float4(o.a[3], o.a[4], o.a[5], o.a[7]);
+  a.cpos[c] = o.pos;
+  a.cattr[2 * (size_t)c] = make_float4(o.a[0], o.a[1], o.a[2], o.a[6]);
+  a.cattr[2 * (size_t)c + 1] = make_float4(o.a[3], o.a[4], o.a[5], o.a[7]);
 }
 
-__device__ Corner load_corner(const MeshArgs& a, size_t c) {
-  const float4 p = a.corners[3 * c], q = a.corners[3 * c + 1], r = a.corners[3 * c + 2];
-  Corner o;
-  o.pos = p;
-  o.a[0] = q.x; o.a[1] = q.y; o.a[2] = q.z;
-  o.a[3] = r.x; o.a[4] = r.y; o.a[5] = r.z;
-  o.a[6] = q.w; o.a[7] = r.w;
+template <bool ATTR>
+__device__ CornerT<ATTR> load_corner(const MeshArgs& a, size_t c) {
+  CornerT<ATTR> o;
+  o.pos = a.cpos[c];
+  if (ATTR) {
+    const float4 q = a.cattr[2 * c], r = a.cattr[2 * c + 1];
+    o.a[0] = q.x; o.a[1] = q.y; o.a[2] = q.z;
+    o.a[3] = r.x; o.a[4] = r.y; o.a[5] = r.z;
+    o.a[6] = q.w; o.a[7] = r.w;
+  }
   return o;
 }
 
 // ---------------------------------------------------------------- primitive setup
 __device__ __forceinline__ float lerpf(float x, float y, float t) { return x + t * (y - x); }
-__device__ Corner corner_lerp(const Corner& p, const Corner& q, float t) {
-  Corner o;
+template <bool ATTR>
+__device__ CornerT<ATTR> corner_lerp(const CornerT<ATTR>& p, const CornerT<ATTR>& q, float t) {
+  CornerT<ATTR> o;
   o.pos = make_float4(lerpf(p.pos.x, q.pos.x, t), lerpf(p.pos.y, q.pos.y, t), lerpf(p.pos.z, q.pos.z, t),
                       lerpf(p.pos.w, q.pos.w, t));
-  for (int k = 0; k < 8; k++) o.a[k] = lerpf(p.a[k], q.a[k], t);
+  for (int k = 0; k < nattr(ATTR); k++) o.a[k] = lerpf(p.a[k], q.a[k], t);
   return o;
 }
 // the part of the triangle with z >= 0 (0, 3 or 4 corners, in order)
-__device__ int clip_near(const Corner* c, Corner* out) {
+template <bool ATTR>
+__device__ int clip_near(const CornerT<ATTR>* c, CornerT<ATTR>* out) {
   int n = 0;
   for (int i = 0; i < 3; i++) {
-    const Corner& p = c[i];
-    const Corner& q = c[i == 2 ? 0 : i + 1];
+    const CornerT<ATTR>& p = c[i];
+    const CornerT<ATTR>& q = c[i == 2 ? 0 : i + 1];
     const bool inp = p.pos.z >= 0.0f, inq = q.pos.z >= 0.0f;
     if (inp) out[n++] = p;
     if (inp != inq) out[n++] = corner_lerp(p, q, p.pos.z / (p.pos.z - q.pos.z));
@@ -182,12 +191,14 @@ __device__ int clip_near(const Corner* c, Corner* out) {
   return n;
 }
 
-struct SVtx {
+template <bool ATTR>
+struct SVtxT {
   float X, Y, nz, iw;
-  float a[8];
+  float a[ATTR ? 8 : 1];
 };
-struct Tri {
-  SVtx v[3];
+template <bool ATTR>
+struct TriT {
+  SVtxT<ATTR> v[3];
   float sg, aa, bias;
   bool own0, own1, own2;
   int x0, x1, y0, y1;
@@ -209,38 +220,49 @@ struct Tri {
     const float q0 = b0 * v[0].iw, q1 = b1 * v[1].iw, q2 = b2 * v[2].iw;
     const float qs = q0 + q1 + q2;
     const float w0 = q0 / qs, w1 = q1 / qs, w2 = q2 / qs;
-    for (int k = 0; k < 8; k++) out[k] = w0 * v[0].a[k] + w1 * v[1].a[k] + w2 * v[2].a[k];
+    for (int k = 0; k < nattr(ATTR); k++) out[k] = w0 * v[0].a[k] + w1 * v[1].a[k] + w2 * v[2].a[k];
   }
 };
+using Tri = TriT<true>;
 __device__ __forceinline__ bool edge_owned(float dx, float dy) { return dy > 0.0f || (dy == 0.0f && dx < 0.0f); }
 
-__device__ SVtx screen(const Corner& c, uint32_t W, uint32_t H) {
-  SVtx v;
+template <bool ATTR>
+__device__ SVtxT<ATTR> screen(const CornerT<ATTR>& c, uint32_t W, uint32_t H) {
+  SVtxT<ATTR> v;
   const float nx = c.pos.x / c.pos.w, ny = c.pos.y / c.pos.w;
   v.nz = c.pos.z / c.pos.w;
   v.X = (nx * 0.5f + 0.5f) * (float)W;
   v.Y = (0.5f - ny * 0.5f) * (float)H;
   v.iw = 1.0f / c.pos.w;
-  for (int k = 0; k < 8; k++) v.a[k] = c.a[k];
+  for (int k = 0; k < nattr(ATTR); k++) v.a[k] = c.a[k];
   return v;
 }
 
 // Part s (0 or 1) of triangle tl of draw d, ready to rasterize; false when it
 // has no fragments (outside the near plane, w <= 0, zero or NaN area).
-__device__ bool setup_tri(const MeshArgs& a, const MeshDraw& d, uint32_t tl, int s, Tri& T) {
-  Corner c[3], poly[4];
+template <bool ATTR>
+__device__ bool setup_tri(const MeshArgs& a, const MeshDraw& d, uint32_t tl, int s, TriT<ATTR>& T) {
   const size_t c0 = (size_t)d.corner_base + 3 * (size_t)tl;
-  for (int k = 0; k < 3; k++) c[k] = load_corner(a, c0 + k);
-  const int np = clip_near(c, poly);
-  if (s + 2 >= np) return false;
-  const Corner* t0 = &poly[0];
-  const Corner* t1 = &poly[s + 1];
-  const Corner* t2 = &poly[s + 2];
-  if (!(t0->pos.w > 0.0f && t1->pos.w > 0.0f && t2->pos.w > 0.0f)) return false;
-  T.v[0] = screen(*t0, a.w, a.h);
-  T.v[1] = screen(*t1, a.w, a.h);
-  T.v[2] = screen(*t2, a.w, a.h);
-  const SVtx* v = T.v;
+  const CornerT<ATTR> c0v = load_corner<ATTR>(a, c0), c1v = load_corner<ATTR>(a, c0 + 1),
+                      c2v = load_corner<ATTR>(a, c0 + 2);
+  if (c0v.pos.z >= 0.0f && c1v.pos.z >= 0.0f && c2v.pos.z >= 0.0f) {  // nothing to clip (kept in registers)
+    if (s != 0 || !(c0v.pos.w > 0.0f && c1v.pos.w > 0.0f && c2v.pos.w > 0.0f)) return false;
+    T.v[0] = screen(c0v, a.w, a.h);
+    T.v[1] = screen(c1v, a.w, a.h);
+    T.v[2] = screen(c2v, a.w, a.h);
+  } else {
+    CornerT<ATTR> c[3] = {c0v, c1v, c2v}, poly[4];
+    const int np = clip_near<ATTR>(c, poly);
+    if (s + 2 >= np) return false;
+    const CornerT<ATTR>* t0 = &poly[0];
+    const CornerT<ATTR>* t1 = &poly[s + 1];
+    const CornerT<ATTR>* t2 = &poly[s + 2];
+    if (!(t0->pos.w > 0.0f && t1->pos.w > 0.0f && t2->pos.w > 0.0f)) return false;
+    T.v[0] = screen(*t0, a.w, a.h);
+    T.v[1] = screen(*t1, a.w, a.h);
+    T.v[2] = screen(*t2, a.w, a.h);
+  }
+  const SVtxT<ATTR>* v = T.v;
   const float A = (v[1].X - v[0].X) * (v[2].Y - v[0].Y) - (v[2].X - v[0].X) * (v[1].Y - v[0].Y);
   if (!(A > 0.0f) && !(A < 0.0f)) return false;
   T.sg = A > 0.0f ? 1.0f : -1.0f;
@@ -327,8 +349,8 @@ __device__ __forceinline__ unsigned long long vis_key(float z, uint32_t seq) {
 // ---------------------------------------------------------------- rasterization
 // Every pixel of the rectangle [x0, x1] x [y0, y1] (within T's bounding box),
 // strided over `lanes` threads.
-template <class Op>
-__device__ void raster(const Tri& T, int x0, int x1, int y0, int y1, int lane, int lanes, Op op) {
+template <bool ATTR, class Op>
+__device__ void raster(const TriT<ATTR>& T, int x0, int x1, int y0, int y1, int lane, int lanes, Op op) {
   const int bw = x1 - x0 + 1;
   const int n = bw * (y1 - y0 + 1);
   for (int i = lane; i < n; i += lanes) {
@@ -343,23 +365,27 @@ __device__ void raster(const Tri& T, int x0, int x1, int y0, int y1, int lane, i
 }
 
 // The visibility operation of the opaque draws: 'less' against the depth the
-// run of opaque draws started from, alpha-cut fragments excluded.
+// run of opaque draws started from; with ATTR the fragment's alpha cut too.
+template <bool ATTR>
 struct OpaqueOp {
   const MeshArgs* a;
   const MeshDraw* d;
-  const Tri* T;
+  const TriT<ATTR>* T;
   uint32_t seq;
   __device__ void operator()(int px, int py, const float* e, float z) const {
     const size_t p = (size_t)py * a->w + (size_t)px;
     if (!(z < a->depth[p])) return;
-    if (d->alpha_cut > 0.0f && mesh_fs(*a, *d, *T, px, py, e).discarded) return;
+    if constexpr (ATTR) {
+      if (mesh_fs(*a, *d, *T, px, py, e).discarded) return;
+    }
     atomicMin(a->keys + p, vis_key(z, seq));
   }
 };
 // The decal test: biased depth, clamped to [0, 1], 'less-equal'; counted or collected.
+template <bool ATTR>
 struct DecalOp {
   const MeshArgs* a;
-  const Tri* T;
+  const TriT<ATTR>* T;
   uint32_t seq;
   bool fill;
   __device__ void operator()(int px, int py, const float*, float z) const {
@@ -372,16 +398,44 @@ struct DecalOp {
   }
 };
 
-// kind 0: opaque visibility, 1: decal count, 2: decal fill
-template <int KIND>
-__device__ void raster_part(const MeshArgs& a, const MeshDraw& d, const Tri& T, uint32_t tri, int s, int x0, int x1,
-                            int y0, int y1, int lane, int lanes) {
+// kind 0: opaque visibility, 1: decal count, 2: decal fill.  ATTR: the
+// varyings are loaded (an opaque draw with an alpha cut shades in this pass).
+template <int KIND, bool ATTR>
+__device__ void raster_part(const MeshArgs& a, const MeshDraw& d, const TriT<ATTR>& T, uint32_t tri, int s, int x0,
+                            int x1, int y0, int y1, int lane, int lanes) {
   const uint32_t seq = tri * 2u + (uint32_t)s;
-  if (KIND == 0) raster(T, x0, x1, y0, y1, lane, lanes, OpaqueOp{&a, &d, &T, seq});
-  else raster(T, x0, x1, y0, y1, lane, lanes, DecalOp{&a, &T, seq, KIND == 2});
+  if (KIND == 0) raster(T, x0, x1, y0, y1, lane, lanes, OpaqueOp<ATTR>{&a, &d, &T, seq});
+  else raster(T, x0, x1, y0, y1, lane, lanes, DecalOp<ATTR>{&a, &T, seq, KIND == 2});
 }
-__device__ __forceinline__ uint32_t tiles_x(const Tri& T) { return (uint32_t)(T.x1 - T.x0 + TILE) / TILE; }
-__device__ __forceinline__ uint32_t tiles_y(const Tri& T) { return (uint32_t)(T.y1 - T.y0 + TILE) / TILE; }
+template <bool ATTR>
+__device__ __forceinline__ uint32_t tiles_x(const TriT<ATTR>& T) { return (uint32_t)(T.x1 - T.x0 + TILE) / TILE; }
+template <bool ATTR>
+__device__ __forceinline__ uint32_t tiles_y(const TriT<ATTR>& T) { return (uint32_t)(T.y1 - T.y0 + TILE) / TILE; }
+
+template <int KIND, bool ATTR>
+__device__ void raster_triangle(const MeshArgs& a, const MeshDraw& d, uint32_t tri) {
+  for (int s = 0; s < 2; s++) {
+    TriT<ATTR> T;
+    if (!setup_tri(a, d, tri - d.tri_base, s, T)) continue;
+    if ((T.x1 - T.x0 + 1) * (T.y1 - T.y0 + 1) > BIG_PIXELS) {
+      const unsigned long long old = atomicAdd(a.big_count, (1ull << 32) | (tiles_x(T) * tiles_y(T)));
+      const uint32_t slot = (uint32_t)(old >> 32);
+      if (slot < a.big_cap) a.big[slot] = make_uint4(tri, (uint32_t)s, (uint32_t)old, 0u);  // never full: 2 per triangle
+      continue;
+    }
+    raster_part<KIND, ATTR>(a, d, T, tri, s, T.x0, T.x1, T.y0, T.y1, 0, 1);
+  }
+}
+
+template <int KIND, bool ATTR>
+__device__ void raster_tile(const MeshArgs& a, const MeshDraw& d, uint4 b, uint32_t u) {
+  TriT<ATTR> T;
+  if (!setup_tri(a, d, b.x - d.tri_base, (int)b.y, T)) return;
+  const uint32_t t = u - b.z, tx = tiles_x(T);
+  const int x0 = T.x0 + (int)(t % tx) * TILE, y0 = T.y0 + (int)(t / tx) * TILE;
+  raster_part<KIND, ATTR>(a, d, T, b.x, (int)b.y, x0, min(x0 + TILE - 1, T.x1), y0, min(y0 + TILE - 1, T.y1),
+                          threadIdx.x, blockDim.x);
+}
 
 // One thread per triangle of draws [d0, d1).  A large footprint is deferred as
 // TILE x TILE tiles: one 64-bit atomic gives the part its list slot (high word)
@@ -392,17 +446,8 @@ __global__ void mesh_raster_kernel(const MeshArgs a, uint32_t d0, uint32_t d1, u
   const uint32_t tri = tri0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (tri >= tri1) return;
   const MeshDraw& d = a.draws[find_draw(a, d0, d1, tri)];
-  for (int s = 0; s < 2; s++) {
-    Tri T;
-    if (!setup_tri(a, d, tri - d.tri_base, s, T)) continue;
-    if ((T.x1 - T.x0 + 1) * (T.y1 - T.y0 + 1) > BIG_PIXELS) {
-      const unsigned long long old = atomicAdd(a.big_count, (1ull << 32) | (tiles_x(T) * tiles_y(T)));
-      const uint32_t slot = (uint32_t)(old >> 32);
-      if (slot < a.big_cap) a.big[slot] = make_uint4(tri, (uint32_t)s, (uint32_t)old, 0u);  // never full: 2 per triangle
-      continue;
-    }
-    raster_part<KIND>(a, d, T, tri, s, T.x0, T.x1, T.y0, T.y1, 0, 1);
-  }
+  if (KIND == 0 && d.alpha_cut > 0.0f) raster_triangle<KIND, true>(a, d, tri);
+  else raster_triangle<KIND, false>(a, d, tri);
 }
 
 // The tiles of the deferred large triangles, a block each (grid-strided).
@@ -418,12 +463,8 @@ __global__ void mesh_raster_big_kernel(const MeshArgs a, uint32_t d0, uint32_t d
     }
     const uint4 b = a.big[lo];
     const MeshDraw& d = a.draws[find_draw(a, d0, d1, b.x)];
-    Tri T;
-    if (!setup_tri(a, d, b.x - d.tri_base, (int)b.y, T)) continue;
-    const uint32_t t = u - b.z, tx = tiles_x(T);
-    const int x0 = T.x0 + (int)(t % tx) * TILE, y0 = T.y0 + (int)(t / tx) * TILE;
-    raster_part<KIND>(a, d, T, b.x, (int)b.y, x0, min(x0 + TILE - 1, T.x1), y0, min(y0 + TILE - 1, T.y1),
-                      threadIdx.x, blockDim.x);
+    if (KIND == 0 && d.alpha_cut > 0.0f) raster_tile<KIND, true>(a, d, b, u);
+    else raster_tile<KIND, false>(a, d, b, u);
   }
 }
 

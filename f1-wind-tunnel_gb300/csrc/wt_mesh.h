@@ -42,7 +42,8 @@ struct MeshArgs {
   const float4* rig;        // the Rig uniform, 87 vec4
   // frame
   uint32_t w, h;
-  float4* corners;          // vertex shader outputs: 3 float4 per corner
+  float4* cpos;             // vertex shader outputs per corner: clip position,
+  float4* cattr;            // and 2 float4 of varyings (world xyz + u, normal xyz + v)
   float* depth;             // depth32float
   unsigned long long* keys; // visibility: depth bits << 32 | triangle sequence * 2 + part
   uint4* big;               // parts with a large footprint: (triangle, part, first tile, 0)
