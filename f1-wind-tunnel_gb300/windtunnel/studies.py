@@ -4,8 +4,8 @@
         generate the training set (seeded 256x96x80 F1 runs, fields averaged
         late in the run), train the network on the GPU with libwt's kernels and
         save the weights.
-    python -m windtunnel.studies judge --weights FILE [--small] --out DIR
-        warm vs cold FP32 starts of held-out seeds, judged by the LBM.
+    python -m windtunnel.studies evaluate --weights FILE [--small] --out DIR
+        warm vs cold FP32 starts of held-out seeds, evaluated by the LBM.
     python -m windtunnel.studies sweep --weights FILE [--small] --out DIR
         the 25-point ride-height aero map plus 8 uneven lattices: time to 1 %
         convergence of every case's windowed Cd and Cl, plain FP32 cold start
@@ -61,7 +61,7 @@ def warm_fields(model, shapes):
     return [ws.denormalize(p) for p in P]
 
 
-def judge(model, seeds, steps, group=64, storage="f32"):
+def evaluate(model, seeds, steps, group=64, storage="f32"):
     """Cold and warm runs of the held-out seeds: per-seed convergence steps."""
     shapes = [ws.case_shape(s) for s in seeds]
     cases = [(ws.F1_DIMS, ws.F1_H, sh) for sh in shapes]
@@ -78,7 +78,7 @@ def judge(model, seeds, steps, group=64, storage="f32"):
     return rows, cold, warm
 
 
-def summarize_judge(rows, horizon):
+def summarize_evaluation(rows, horizon):
     cold = np.array([r["cold_steps"] if r["cold_steps"] is not None else horizon for r in rows], float)
     warm = np.array([r["warm_steps"] if r["warm_steps"] is not None else horizon for r in rows], float)
     cold_cd = np.array([r["cold_steps_cd"] if r["cold_steps_cd"] is not None else horizon for r in rows], float)
@@ -92,7 +92,7 @@ def summarize_judge(rows, horizon):
 
 
 def study_warmstart(args):
-    """Training set, training, validation loss and weights (the judge is separate)."""
+    """Training set, training, validation loss and weights (the LBM evaluation is `evaluate`)."""
     os.makedirs(args.out, exist_ok=True)
     small = args.small
     n_train, n_val = (16, 4) if small else (args.train_cases, args.val_cases)
@@ -123,17 +123,17 @@ def study_warmstart(args):
         json.dump(res, f, indent=1)
 
 
-def study_judge(args):
-    """Held-out seeds: cold and warm FP32 runs judged by the LBM."""
+def study_evaluate(args):
+    """Held-out seeds: cold and warm FP32 runs evaluated by the LBM."""
     os.makedirs(args.out, exist_ok=True)
     model = load_model(args.weights)
     seeds = list(range(5000, 5000 + (2 if args.small else args.val_cases)))
-    horizon = 4000 if args.small else args.judge_steps
-    rows, cold, warm = judge(model, seeds, horizon)
-    summary = summarize_judge(rows, horizon)
-    log(f"judge: {summary}")
-    with open(os.path.join(args.out, "warmstart_judge.json"), "w") as f:
-        json.dump({"horizon": horizon, "window": ws.WINDOW, "tolerance": ws.TOLERANCE, "judge": rows,
+    horizon = 4000 if args.small else args.eval_steps
+    rows, cold, warm = evaluate(model, seeds, horizon)
+    summary = summarize_evaluation(rows, horizon)
+    log(f"evaluation: {summary}")
+    with open(os.path.join(args.out, "warmstart_eval.json"), "w") as f:
+        json.dump({"horizon": horizon, "window": ws.WINDOW, "tolerance": ws.TOLERANCE, "cases": rows,
                    "summary": summary}, f, indent=1)
     # trailing-window means every 64 steps (the per-step series would be too large to keep)
     series = {}
@@ -141,7 +141,7 @@ def study_judge(args):
         for tag, run in (("cold", cold), ("warm", warm)):
             series[f"{tag}_cd_{r['seed']}"] = ws.trailing_mean(run["cd"][i])[63::64].astype(np.float32)
             series[f"{tag}_cl_{r['seed']}"] = ws.trailing_mean(run["cl"][i])[63::64].astype(np.float32)
-    np.savez_compressed(os.path.join(args.out, "judge_window_means.npz"), **series)
+    np.savez_compressed(os.path.join(args.out, "eval_window_means.npz"), **series)
 
 
 def single_lattice_step_s(dims, h, shape, steps=2048):
@@ -179,7 +179,7 @@ def study_sweep(args):
     after another (single-lattice launches) vs batched FP16 with the warm start."""
     os.makedirs(args.out, exist_ok=True)
     cases, labels = sweep_cases(args.small)
-    horizon = 4000 if args.small else args.judge_steps
+    horizon = 4000 if args.small else args.eval_steps
     model = load_model(args.weights)
     log(f"{len(cases)} cases, horizon {horizon} steps")
     # cold FP32 reference runs (batched for the study's own speed; the sequential
@@ -219,21 +219,21 @@ def study_sweep(args):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["warmstart", "judge", "sweep"])
+    ap.add_argument("study", choices=["warmstart", "evaluate", "sweep"])
     ap.add_argument("--train-cases", type=int, default=400)
     ap.add_argument("--val-cases", type=int, default=50)
     ap.add_argument("--settle", type=int, default=24000)
     ap.add_argument("--average", type=int, default=8000)
-    ap.add_argument("--out", default="gpurun_out/study")
+    ap.add_argument("--out", default="study_out")
     ap.add_argument("--small", action="store_true")
     ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--judge-steps", type=int, default=64000)
+    ap.add_argument("--eval-steps", type=int, default=64000)
     ap.add_argument("--weights", default=None)
     args = ap.parse_args(argv)
     import torch
     torch.cuda.set_device(0)
-    {"warmstart": study_warmstart, "judge": study_judge, "sweep": study_sweep}[args.study](args)
+    {"warmstart": study_warmstart, "evaluate": study_evaluate, "sweep": study_sweep}[args.study](args)
 
 
 if __name__ == "__main__":

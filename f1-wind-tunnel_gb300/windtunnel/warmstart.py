@@ -1,4 +1,4 @@
-"""Learned warm start of the aero-map cases and its judge.
+"""Learned warm start of the aero-map cases and its evaluation.
 
 * Features: the car's signed distance sampled on the coarse 64x24x20 grid over
   the tunnel (wt_sdf_sample), the front and rear ride heights, the three wing

@@ -1,4 +1,4 @@
-"""What the trained warm start gains over the cold start, judged by the LBM.
+"""What the trained warm start gains over the cold start, evaluated by the LBM.
 
 The committed network (windtunnel/data/warmstart_f1.npz, trained on seeds
 1000-1399) predicts the coarse flow of two held-out cars (seeds 5000 and 5003);
