@@ -37,6 +37,7 @@ class CarModel:
     parts: np.ndarray      # [nz, ny, nx] uint16 binary16 bits: the parts atlas
     parts_dims: tuple      # (nx, ny, nz)
     rig: np.ndarray        # [87, 4] float32: the Rig uniform
+    rig_data: dict = None  # the rig JSON (w17.rig.json), so setShape can rebuild the Rig uniform
 
 
 def rig_uniform(rig, angles, rear_twist=0.0, flap_scale=1.0, pod_squeeze=0.0, fly=(0.0, 0.0, 1.0, 1.0)):
@@ -100,7 +101,7 @@ def load_w17(models_dir, p, fly_progress=(0.0, 0.0)):
     with open(os.path.join(models_dir, "w17.rig.json")) as f:
         rig = json.load(f)
     atlas, dims = parts_atlas(rig, np.fromfile(os.path.join(models_dir, "w17.parts.bin"), np.uint16))
-    return CarModel(sdf.reshape(sz, sy, sx), atlas, dims, w17_rig(rig, p, fly_progress))
+    return CarModel(sdf.reshape(sz, sy, sx), atlas, dims, w17_rig(rig, p, fly_progress), rig)
 
 
 # ---------------------------------------------------------------- synthetic stand-in
@@ -182,4 +183,4 @@ def synthetic_w17(p=None, fly_progress=(0.0, 0.0)):
             d = np.minimum(d, _round_box(gx, gy, gz, c, b, 0.005))
         data.append(_to_half_bits(d).ravel())
     atlas, dims = parts_atlas(rig, np.concatenate(data))
-    return CarModel(_to_half_bits(body), atlas, dims, w17_rig(rig, p, fly_progress))
+    return CarModel(_to_half_bits(body), atlas, dims, w17_rig(rig, p, fly_progress), rig)

@@ -210,7 +210,17 @@ class AeroEngine:
         self._check(self.lib.wt_reset(self.ctx), "wt_reset")
 
     def set_shape(self, p: ShapeParams):
+        """setShape (engine.ts:426-470): for the W17 scene the Rig uniform follows
+        the wing settings of p (engine.ts:450-462) when the car model carries
+        its rig data; then voxelize."""
         self.shape_params = p
+        model = getattr(self, "car_model", None)
+        if p.kind == ShapeKind.W17 and model is not None and model.rig_data is not None:
+            from dataclasses import replace
+            from .car_model import w17_rig
+            rig = w17_rig(model.rig_data, p, tuple(getattr(self, "fly", (0.0, 0.0))))
+            if not np.array_equal(rig, model.rig):
+                self.set_car_model(replace(model, rig=rig))
         self.set_shape_raw(pack_shape(p))
 
     def set_car_model(self, model):

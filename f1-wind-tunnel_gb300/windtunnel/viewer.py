@@ -95,6 +95,7 @@ class Viewer:
         self.flow_time = 0.0
         self.view = ViewParams()
         self.mesh = None   # the car mesh the W17 scene draws into the G-buffer (engine.ts:679)
+        self.fly = [0.0, 0.0]  # fly-away progress of the front and rear wing (engine.ts:192-193)
 
     def _quality(self):
         for q, d in QUALITIES.items():
@@ -177,9 +178,33 @@ class Viewer:
         s.time = self.flow_time
         return s
 
+    def animate_wings(self, dt):
+        """animateWings (engine.ts:395-408): a detached wing flies off at 0.75 per
+        second and a refitted one returns at 1.4 per second; the result only
+        moves the mesh (the distance field keeps the rig of the last setShape)."""
+        p = self.engine.shape_params
+        target = (0.0 if p.frontWingOn else 1.0, 0.0 if p.rearWingOn else 1.0)
+        for i in (0, 1):
+            if abs(target[i] - self.fly[i]) < 1e-4:
+                continue
+            self.fly[i] = min(1.0, self.fly[i] + dt * 0.75) if target[i] > self.fly[i] else \
+                max(0.0, self.fly[i] - dt * 1.4)
+        self.engine.fly = tuple(self.fly)  # the progress the next setShape builds its rig with
+
+    def mesh_rig(self):
+        """The Rig uniform the mesh is drawn with: the model's, with the current fly-away progress."""
+        rig = np.array(self.engine.car_model.rig, np.float32)
+        rig[74, 0:2] = self.fly
+        return rig
+
     # -- frame(target, cam, steps, dt) ----------------------------------------------
     def frame(self, cam, steps=8, dt=1.0 / 60):
         e, v = self.engine, self.view
+        p = e.shape_params
+        mesh_mode = (self.mesh is not None and p is not None and p.kind == ShapeKind.W17 and
+                     getattr(e, "car_model", None) is not None)
+        if mesh_mode:
+            self.animate_wings(dt)
         self.flow_time += dt * self.visual_flow_rate()
         even = max(2, steps - steps % 2)
         color_mode = 0 if v.color_field == ColorField.Vorticity else v.color_field
@@ -208,12 +233,9 @@ class Viewer:
                          slice_axis=v.slice_axis, slice_pos=v.slice_pos, paint=v.livery.paint,
                          accent=v.livery.accent, carbon=v.livery.carbon,
                          cooling=e.shape_params.cooling if e.shape_params is not None else 1)
-        p = e.shape_params
-        mesh_mode = (self.mesh is not None and p is not None and p.kind == ShapeKind.W17 and
-                     getattr(e, "car_model", None) is not None)
         self.renderer.frame(cam, look, view, dt, v.kmh, parts, color_mode, v.flow_mode == FlowMode.Smoke, lines,
                             self.flow_time, v.flow_mode == FlowMode.Vortices, mesh=self.mesh if mesh_mode else None,
-                            rig=e.car_model.rig if mesh_mode else None, params=p)
+                            rig=self.mesh_rig() if mesh_mode else None, params=p)
 
     def image(self):
         return self.renderer.read(TARGET_OUTPUT)

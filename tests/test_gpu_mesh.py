@@ -110,3 +110,19 @@ def test_mesh_errors(setup):
     t = np.zeros(3, np.uint8)
     m = ctypes.c_void_p()
     assert lib.wt_mesh_create(e.ctx, v.ctypes.data, 3, i.ctypes.data, 3, t.ctypes.data, ctypes.byref(m)) != 0
+
+
+def test_set_shape_rebuilds_the_rig(setup):
+    """setShape hands the W17 rig of the new wing settings to the scene (engine.ts:450-462)."""
+    from windtunnel.car_model import synthetic_w17
+    from windtunnel.engine import ShapeKind, ShapeParams
+    mc, z, e, mesh, c = setup
+    p0 = ShapeParams(kind=ShapeKind.W17)
+    p1 = ShapeParams(kind=ShapeKind.W17, frontFlapDeg=9.0, rearWing=1, thinWings=True)
+    e.set_car_model(synthetic_w17(p0))
+    e.set_shape(p1)
+    assert np.array_equal(e.car_model.rig, synthetic_w17(p1).rig)
+    d1 = e.debug_read()["solid"].copy()
+    e.set_car_model(synthetic_w17(p1))
+    e.set_shape(p1)
+    assert np.array_equal(e.debug_read()["solid"], d1)

@@ -221,3 +221,27 @@ def test_w17_assets_build_the_mesh(wt_lib):
     for i in small[:6]:
         w, h, rgba = decode_png(scene.images[i][1])
         assert rgba.shape == (h, w, 4) and rgba.dtype == np.uint8
+
+
+def test_wing_fly_away_animation():
+    """animateWings (engine.ts:395-408) as the viewer runs it for the mesh rig."""
+    from types import SimpleNamespace
+    from windtunnel.car_model import synthetic_w17
+    from windtunnel.engine import ShapeKind, ShapeParams
+    from windtunnel.viewer import Viewer
+    p = ShapeParams(kind=ShapeKind.W17, frontWingOn=False)
+    v = Viewer.__new__(Viewer)
+    v.fly = [0.0, 0.0]
+    v.engine = SimpleNamespace(shape_params=p, car_model=synthetic_w17(p))
+    for _ in range(30):
+        v.animate_wings(1 / 60)
+    assert v.fly[0] == pytest.approx(30 / 60 * 0.75) and v.fly[1] == 0.0
+    for _ in range(200):
+        v.animate_wings(1 / 60)
+    # it stops within 1e-4 of the target, as the engine's loop does
+    assert v.fly[0] == pytest.approx(1.0, abs=1e-4) and v.fly[1] == 0.0 and v.engine.fly == tuple(v.fly)
+    rig = v.mesh_rig()
+    assert rig[74].tolist() == pytest.approx([1.0, 0.0, 0.0, 1.0], abs=1e-4)  # progress; front off, rear fitted
+    v.engine.shape_params = ShapeParams(kind=ShapeKind.W17)   # refitted: back at 1.4 per second
+    v.animate_wings(0.5)
+    assert v.fly[0] == pytest.approx(0.3)
