@@ -19,6 +19,7 @@ material targets:
   close    camera inside the front wing's span: triangles cross the near plane
   under    low camera under the floor (two large triangles), 97x61
 Composites: hero and rig (scene target, binary16), cooling 1 and 2.
+Plus `edge`: a small mesh of the pipeline's corner cases (edge_mesh), 80x48.
 
 Needs the reference checkout (build container only).
 """
@@ -59,6 +60,65 @@ def cases():
     ]
 
 
+def edge_mesh():
+    """A small mesh of the pipeline's corner cases, in MeshCar's formats: a wall of
+    two triangles larger than the view (the tiled path), two coplanar quads in
+    different draws (z-fighting: per pixel the smaller rounded depth wins, an
+    exact tie goes to the first drawn), two decal layers in the same plane
+    (blended in draw order, one textured with an alpha ramp), a zero-area triangle,
+    one wholly behind the camera and one crossing the near plane, a draw whose
+    count is not a multiple of 3 and an empty draw."""
+    from windtunnel.mesh_car import DrawSpec, MeshData
+    v = []
+
+    def quad(p0, p1, p2, p3, n=(0.0, 0.0, -1.0)):
+        base = len(v)
+        for (x, y, z), (u, w) in zip((p0, p1, p2, p3), ((0, 0), (1, 0), (1, 1), (0, 1))):
+            v.append([x, y, z, u, n[0], n[1], n[2], w])
+        return [base, base + 1, base + 2, base + 0, base + 2, base + 3]
+    wall = quad((-30.0, -20.0, 6.0), (30.0, -20.0, 6.0), (30.0, 20.0, 6.0), (-30.0, 20.0, 6.0))
+    q_a = quad((-1.0, -0.5, 2.0), (0.5, -0.5, 2.0), (0.5, 0.8, 2.0), (-1.0, 0.8, 2.0))
+    q_b = quad((-0.5, -0.8, 2.0), (1.0, -0.8, 2.0), (1.0, 0.5, 2.0), (-0.5, 0.5, 2.0))
+    d_a = quad((-0.8, -0.3, 2.0), (0.3, -0.3, 2.0), (0.3, 0.6, 2.0), (-0.8, 0.6, 2.0))
+    d_b = quad((-0.3, -0.6, 2.0), (0.8, -0.6, 2.0), (0.8, 0.3, 2.0), (-0.3, 0.3, 2.0))
+    b = len(v)
+    v += [[0.2, 0.2, 1.0, 0, 0, 0, -1, 0], [0.4, 0.4, 1.0, 1, 0, 0, -1, 0], [0.6, 0.6, 1.0, 0, 0, 0, -1, 1]]
+    degenerate = [b, b + 1, b + 2]
+    b = len(v)
+    v += [[0.0, 0.0, -2.0, 0, 0, 0, -1, 0], [1.0, 0.0, -2.0, 1, 0, 0, -1, 0], [0.0, 1.0, -2.0, 0, 0, 0, -1, 1]]
+    behind = [b, b + 1, b + 2]
+    b = len(v)
+    v += [[-0.6, -0.6, -0.5, 0, 0, 0, -1, 0], [0.6, -0.4, 3.0, 1, 0, 0, -1, 0], [0.1, 0.7, 3.0, 0, 0, 0, -1, 1]]
+    crossing = [b, b + 1, b + 2]
+    groups = [("wall", wall), ("quad_a", q_a), ("quad_b", q_b + degenerate + behind), ("crossing", crossing + [0]),
+              ("decal_a", d_a), ("decal_b", d_b)]
+    idx, ranges = [], {}
+    for name, ii in groups:
+        ranges[name] = (len(idx), len(ii))
+        idx += ii
+    verts = np.array(v, np.float32)
+    tex = np.zeros((8, 8, 4), np.uint8)
+    tex[..., 0] = 200
+    tex[..., 3] = np.arange(8, dtype=np.uint8)[None, :] * 36
+    m = dict(metal=0.2, rough=0.4, coat=0.2, emissive=0.0, is_body=0.0)
+    draws = [
+        DrawSpec("wall", (0.3, 0.3, 0.3, 1.0), alpha_cut=0.0, first=ranges["wall"][0], count=6, **m),
+        DrawSpec("quad_a", (0.9, 0.1, 0.1, 1.0), alpha_cut=0.0, first=ranges["quad_a"][0], count=6, **m),
+        DrawSpec("empty", (1.0, 1.0, 1.0, 1.0), alpha_cut=0.0, first=0, count=0, **m),
+        DrawSpec("quad_b", (0.1, 0.9, 0.1, 1.0), alpha_cut=0.0, first=ranges["quad_b"][0], count=12, **m),
+        DrawSpec("crossing", (0.1, 0.1, 0.9, 1.0), alpha_cut=0.0, first=ranges["crossing"][0], count=4, **m),
+        DrawSpec("decal_a", (1.0, 1.0, 1.0, 0.7), alpha_cut=0.02, first=ranges["decal_a"][0], count=6, texture=0,
+                 blend=True, **m),
+        DrawSpec("decal_b", (0.2, 0.4, 1.0, 0.6), alpha_cut=0.02, first=ranges["decal_b"][0], count=6, blend=True, **m),
+    ]
+    return MeshData(verts, np.array(idx, np.uint32), np.zeros(len(v), np.uint8), draws, [(8, 8, tex)])
+
+
+def edge_camera():
+    """Looking down +z from the origin (so the wall and quads face it)."""
+    return R.orbit_camera((0.0, 0.0, 1.0), -np.pi / 2, 0.0, 1.0, 80 / 48)
+
+
 def frame_halton(k):
     k = (k % 8) + 1
     return R.halton(k, 2) - 0.5, R.halton(k, 3) - 0.5
@@ -94,6 +154,13 @@ def main():
                 out[f"{name}_scene_c{cooling}"] = sc.astype(np.float16)
             po.ref_set_car(None)
             po.ref_set_gbuffer(None, None, None)
+    # the corner-case mesh, 80x48, no rig motion (tags 0, not a body draw)
+    em = edge_mesh()
+    ecam = mesh_cam(edge_camera(), (80, 48), (0.0, 0.0), cases()[0][1])
+    a, n, m, d = po.ref_mesh_gbuffer(em, ecam, synthetic_w17(cases()[0][1]).rig, 80, 48)
+    out.update(edge_verts=em.verts, edge_indices=em.indices, edge_tex=em.textures[0][2],
+               edge_albedo=a, edge_normal=n, edge_material=m)
+    print("edge car texels", int((n[..., 3].astype(np.float32) > 0).sum()))
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 

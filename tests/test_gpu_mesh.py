@@ -69,6 +69,26 @@ def test_gbuffer_bitexact(setup):
             r.close()
 
 
+def test_gbuffer_corner_cases(setup):
+    """Near-plane clipping, a triangle behind the camera, a zero-area one, z-fighting
+    coplanar quads, decal layers in one plane, a wall larger than the view, a
+    ragged and an empty draw (tests/golden/make_mesh.py edge_mesh)."""
+    import make_mesh as mm
+    from windtunnel import render as R
+    from windtunnel.mesh_car import MeshCar, MeshData, mesh_cam
+    mc, z, e, mesh, c = setup
+    em = mm.edge_mesh()
+    data = MeshData(z["edge_verts"], z["edge_indices"], em.tags, em.draws, [(8, 8, z["edge_tex"])])
+    m = MeshCar(e, data)
+    r = R.Renderer(e, 80, 48)
+    try:
+        r.mesh(m, mesh_cam(mm.edge_camera(), (80, 48), (0.0, 0.0), mm.cases()[0][1]), z["hero_rig"])
+        check_gbuffer(r, z, "edge")
+    finally:
+        r.close()
+        m.close()
+
+
 def test_composite_bitexact(setup):
     """Mesh pass, then the scene pass with meshMode over the consumer fixture's
     flow, as Renderer.frame runs them (engine.ts:679-716)."""

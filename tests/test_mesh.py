@@ -121,6 +121,12 @@ def test_reference_reproduces_mesh_fixture():
                                                size[0], size[1], gurney=p.gurney)
         assert same_half(a, z[f"{name}_albedo"]).all() and same_half(n, z[f"{name}_normal"]).all(), name
         assert np.array_equal(m, z[f"{name}_material"]), name
+    em = mm.edge_mesh()
+    assert np.array_equal(em.verts, z["edge_verts"]) and np.array_equal(em.indices, z["edge_indices"])
+    a, n, m, _ = pyoracle.ref_mesh_gbuffer(em, mesh_cam(mm.edge_camera(), (80, 48), (0.0, 0.0), mm.cases()[0][1]),
+                                           z["hero_rig"], 80, 48)
+    assert same_half(a, z["edge_albedo"]).all() and same_half(n, z["edge_normal"]).all()
+    assert np.array_equal(m, z["edge_material"])
 
 
 def test_mesh_fixture_covers_the_pipeline():
