@@ -549,14 +549,22 @@ def main():
     achieved = n * bpl / (kms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
 
-    # ---- end to end through the public API: per-frame parameter upload + force readback
+    # ---- end to end through the public API: per-frame parameter upload + force readback.
+    # Every frame's forces come back to the host, read asynchronously like the
+    # reference's mapped readback (engine.ts:746-760): frame k's copy is collected
+    # while frame k+1 runs, and the last one before the clock stops.
     e2e_frames = max(5, min(args.steps, 100))
     barrier()
     t0 = time.perf_counter()
+    prev = None
     for _ in range(e2e_frames):
         eng.set_sim(sim)                     # Sim uniform + sponge table upload (syncSim, engine.ts:497)
         eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0)
-        eng.read_forces_raw(reset=True)      # maybeReadForces readback (engine.ts:746-747)
+        ticket = eng.read_forces_async(reset=True)   # maybeReadForces readback (engine.ts:746-747)
+        if prev is not None:
+            eng.collect_forces(prev)
+        prev = ticket
+    eng.collect_forces(prev)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = total_cells * lbm_per_frame * e2e_frames / e2e_s / 1e6

@@ -19,6 +19,8 @@
 
 using namespace wt;
 
+#define WT_ASYNC_SLOTS 16  // force readbacks in flight per context
+
 struct wt_renderer;
 struct wt_mesh;
 namespace {
@@ -91,6 +93,11 @@ struct wt_ctx {
   uint32_t car_pdims[3] = {1, 1, 1};
   std::vector<wt_renderer*> renderers;     // live renderers over this lattice
   std::vector<wt_mesh*> meshes;            // live car meshes on this context
+  // asynchronous force readbacks: pinned landing slots, their events, next ticket
+  wt_forces* fpinned = nullptr;
+  wt_forces* fpinned_dev = nullptr;  // the same slots as the device sees them
+  cudaEvent_t fevent[WT_ASYNC_SLOTS] = {};
+  uint64_t fticket = 0;
   std::string err;
 };
 
@@ -510,6 +517,9 @@ int wt_destroy(wt_ctx* c) {
   c->renderers.clear();
   for (wt_mesh* m : c->meshes) release_mesh_buffers(m);
   c->meshes.clear();
+  if (c->fpinned) cudaFreeHost(c->fpinned);
+  for (cudaEvent_t& ev : c->fevent)
+    if (ev) cudaEventDestroy(ev);
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
                   c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters,
@@ -648,23 +658,40 @@ int wt_read_forces(wt_ctx* c, wt_forces* out, int reset) {
   int rc = check_ctx(c);
   if (rc) return rc;
   if (!out) return fail(c, WT_ERR_ARG, "wt_read_forces: null output");
-  if ((rc = flush_forces(c))) return rc;
-  double tot[18];
-  unsigned int g = 0;
-  WT_CUDA(c, cudaMemcpyAsync(tot, c->totals, sizeof(tot), cudaMemcpyDeviceToHost, c->stream));
-  WT_CUDA(c, cudaMemcpyAsync(out->raw, c->raw_totals, 48, cudaMemcpyDeviceToHost, c->stream));
-  WT_CUDA(c, cudaMemcpyAsync(&g, c->counters, 4, cudaMemcpyDeviceToHost, c->stream));
-  WT_CUDA(c, cudaStreamSynchronize(c->stream));
-  memcpy(out->sum, tot, sizeof(out->sum));
-  out->mass = tot[9];
-  out->steps = c->steps_since_read;
-  out->guarded = g;
-  if (reset) {
-    WT_CUDA(c, cudaMemsetAsync(c->totals, 0, 9 * 8, c->stream));
-    WT_CUDA(c, cudaMemsetAsync(c->raw_totals, 0, 48, c->stream));
-    WT_CUDA(c, cudaMemsetAsync(c->counters, 0, 4, c->stream));
-    c->steps_since_read = 0;
+  uint64_t ticket = 0;
+  if ((rc = wt_read_forces_async(c, reset, &ticket))) return rc;
+  return wt_forces_collect(c, ticket, out);
+}
+
+int wt_read_forces_async(wt_ctx* c, int reset, uint64_t* ticket) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!ticket) return fail(c, WT_ERR_ARG, "wt_read_forces_async: null ticket");
+  if (!c->fpinned) {  // landing slots the readout kernel writes directly (host-mapped)
+    WT_CUDA(c, cudaHostAlloc((void**)&c->fpinned, WT_ASYNC_SLOTS * sizeof(wt_forces), cudaHostAllocMapped));
+    WT_CUDA(c, cudaHostGetDevicePointer((void**)&c->fpinned_dev, c->fpinned, 0));
+    for (cudaEvent_t& ev : c->fevent) WT_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   }
+  if ((rc = flush_forces(c))) return rc;
+  const uint32_t slot = (uint32_t)(c->fticket % WT_ASYNC_SLOTS);
+  if (c->fticket >= WT_ASYNC_SLOTS) WT_CUDA(c, cudaEventSynchronize(c->fevent[slot]));  // slot reused
+  WT_CUDA(c, launch_force_readback(c->totals, c->raw_totals, c->counters, c->fpinned_dev + slot, c->steps_since_read,
+                                   reset, c->stream));
+  WT_CUDA(c, cudaEventRecord(c->fevent[slot], c->stream));
+  if (reset) c->steps_since_read = 0;
+  *ticket = c->fticket++;
+  return WT_OK;
+}
+
+int wt_forces_collect(wt_ctx* c, uint64_t ticket, wt_forces* out) {
+  int rc = check_ctx(c);
+  if (rc) return rc;
+  if (!out) return fail(c, WT_ERR_ARG, "wt_forces_collect: null output");
+  if (ticket >= c->fticket || c->fticket - ticket > WT_ASYNC_SLOTS)
+    return fail(c, WT_ERR_ARG, "wt_forces_collect: unknown ticket or overwritten by newer readbacks");
+  const uint32_t slot = (uint32_t)(ticket % WT_ASYNC_SLOTS);
+  WT_CUDA(c, cudaEventSynchronize(c->fevent[slot]));
+  memcpy(out, c->fpinned + slot, sizeof(wt_forces));
   return WT_OK;
 }
 

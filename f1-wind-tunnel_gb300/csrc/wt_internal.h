@@ -109,6 +109,10 @@ struct ReduceArgs {
 };
 cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t nsteps, bool with_mass,
                                 cudaStream_t s);
+// The force accumulators (FP64 totals[10]: sums and mass, raw i32[12], guard
+// counter) into *out, a wt_forces in host-mapped memory; zeroed after if reset.
+cudaError_t launch_force_readback(double* totals, int32_t* raw, unsigned int* counters, wt_forces* out,
+                                  uint64_t steps, int reset, cudaStream_t s);
 cudaError_t launch_read_pop(uint32_t storage, const void* pop, float* out, uint32_t n, uint64_t np, cudaStream_t s);
 cudaError_t launch_write_pop(uint32_t storage, const float* in, void* pop, uint32_t n, uint64_t np, cudaStream_t s);
 // Box average of the fluid cells' (ux, uy, uz, rho) onto a cx x cy x cz grid

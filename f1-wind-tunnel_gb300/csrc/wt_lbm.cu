@@ -892,6 +892,34 @@ cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t
   return cudaGetLastError();
 }
 
+// The force readout in one launch: the accumulators into a wt_forces record
+// (host-mapped memory, so no copy follows) and, with reset, their zeroing.
+// One warp; each lane reads its words before it clears them.
+__global__ void force_readback_kernel(double* totals, int32_t* raw, unsigned int* counters, wt_forces* out,
+                                      uint64_t steps, int reset) {
+  const uint32_t t = threadIdx.x;
+  if (t < 9) {
+    out->sum[t] = totals[t];
+    if (reset) totals[t] = 0.0;
+  }
+  if (t == 9) out->mass = totals[9];
+  if (t < 12) {
+    out->raw[t] = raw[t];
+    if (reset) raw[t] = 0;
+  }
+  if (t == 12) {
+    out->guarded = counters[0];
+    out->steps = steps;
+    if (reset) counters[0] = 0u;
+  }
+}
+
+cudaError_t launch_force_readback(double* totals, int32_t* raw, unsigned int* counters, wt_forces* out,
+                                  uint64_t steps, int reset, cudaStream_t s) {
+  force_readback_kernel<<<1, 32, 0, s>>>(totals, raw, counters, out, steps, reset);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_read_pop(uint32_t storage, const void* pop, float* out, uint32_t n, uint64_t np, cudaStream_t s) {
   return by_storage(storage, [&](auto st) {
     read_pop_kernel<decltype(st)><<<(n + 255) / 256, 256, 0, s>>>(pop, out, n, (uint32_t)np);

@@ -178,6 +178,8 @@ _PROTOS = {
     "wt_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
     "wt_read_forces": (ctypes.c_int, [_vp, ctypes.POINTER(Forces), ctypes.c_int]),
     "wt_read_force_history": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32]),
+    "wt_read_forces_async": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]),
+    "wt_forces_collect": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.POINTER(Forces)]),
     "wt_read_fields": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "wt_read_populations": (ctypes.c_int, [_vp, _vp]),
     "wt_write_state": (ctypes.c_int, [_vp, _vp, _vp, _vp]),

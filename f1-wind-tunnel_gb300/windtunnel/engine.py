@@ -263,6 +263,22 @@ class AeroEngine:
             self.steps_since_read = 0
         return f
 
+    def read_forces_async(self, reset=True):
+        """Queue a force readback without waiting (wt_read_forces_async): returns a
+        ticket for collect_forces."""
+        t = ctypes.c_uint64()
+        self._check(self.lib.wt_read_forces_async(self.ctx, 1 if reset else 0, ctypes.byref(t)),
+                    "wt_read_forces_async")
+        if reset:
+            self.steps_since_read = 0
+        return t.value
+
+    def collect_forces(self, ticket) -> _abi.Forces:
+        """Wait for the readback of `ticket` and return its raw forces."""
+        f = _abi.Forces()
+        self._check(self.lib.wt_forces_collect(self.ctx, ticket, ctypes.byref(f)), "wt_forces_collect")
+        return f
+
     def read_forces(self, kmh=250.0, reset=True):
         """maybeReadForces() scaling (engine.ts:750-759): Newtons, x2 for the mirrored half."""
         f = self.read_forces_raw(reset)

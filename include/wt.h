@@ -173,6 +173,15 @@ int wt_step(wt_ctx* ctx, int n_lbm_steps, int heat_passes, float heat_dt);
  * if reset != 0, zero them (engine.ts:747).  Synchronises the context stream. */
 int wt_read_forces(wt_ctx* ctx, wt_forces* out, int reset);
 
+/* maybeReadForces without waiting, as the reference maps its readback buffer
+ * asynchronously (engine.ts:746-760): queue the pending force reduction, a copy
+ * of the accumulators into one of the context's 16 pinned landing slots and, if
+ * reset != 0, their zeroing; return at once with *ticket.  wt_forces_collect
+ * waits for that copy and fills *out (the same fields as wt_read_forces).  A
+ * ticket can be collected until 16 newer readbacks have been queued. */
+int wt_read_forces_async(wt_ctx* ctx, int reset, uint64_t* ticket);
+int wt_forces_collect(wt_ctx* ctx, uint64_t ticket, wt_forces* out);
+
 /* Per-step FP64 force records of the last `count` steps, oldest first:
  * out[9*k + 3g + c].  count <= min(steps recorded, history_capacity). */
 int wt_read_force_history(wt_ctx* ctx, double* out, uint32_t count);

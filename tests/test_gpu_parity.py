@@ -183,6 +183,37 @@ def test_state_roundtrip_and_history(wt_lib):
     e.close()
 
 
+def test_async_force_readback(wt_lib):
+    """wt_read_forces_async + wt_forces_collect give what wt_read_forces gives,
+    frame after frame, and refuse tickets whose slot was reused."""
+    from windtunnel import AeroEngine, WindTunnelError, f1_config
+    dims, origin, h, sim, shape = f1_config(dims=(64, 24, 20), h=0.18)
+    a = AeroEngine(dims=dims, origin=origin, h=h, sim=sim)
+    b = AeroEngine(dims=dims, origin=origin, h=h, sim=sim)
+    for e in (a, b):
+        e.set_shape_raw(shape)
+    tickets, sync = [], []
+    for k in range(5):
+        for e in (a, b):
+            e.step(8, 2, 4.0)
+        tickets.append(a.read_forces_async(reset=(k % 2 == 0)))
+        sync.append(b.read_forces_raw(reset=(k % 2 == 0)))
+    for t, f in zip(tickets, sync):
+        g = a.collect_forces(t)
+        assert list(g.raw) == list(f.raw) and list(g.sum) == list(f.sum)
+        assert (g.mass, g.steps, g.guarded) == (f.mass, f.steps, f.guarded)
+    assert sync[1].steps == 8 and sync[2].steps == 16
+    first = a.read_forces_async()
+    for _ in range(16):
+        a.read_forces_async()
+    with pytest.raises(WindTunnelError, match="ticket"):
+        a.collect_forces(first)
+    with pytest.raises(WindTunnelError, match="ticket"):
+        a.collect_forces(first + 100)
+    a.close()
+    b.close()
+
+
 def test_full_size_f1_properties(wt_lib):
     """256x96x80 F1 (the benchmark lattice): finite, deterministic run to run,
     per-step force records sum to the accumulator, mass stays near the initial."""
