@@ -71,6 +71,7 @@ struct wt_ctx {
   bool own_stream = true;
   unsigned long long* hist_pos = nullptr;  // device: per-step records written so far
   ReduceArgs* d_reduce = nullptr;          // device: this lattice's reduction record
+  double* red_part = nullptr;              // device: the reduction's chunk sums
   uint32_t bx = 128, by = 1;               // step-kernel block shape
   uint64_t version = 0;                    // bumped whenever kernel arguments change
   // Force records of steps not yet reduced (single-lattice path): the reduction
@@ -212,6 +213,7 @@ ReduceArgs reduce_args(const wt_ctx* c) {
   r.nmass = c->geom.nblocks * warps_per_block(c->geom);
   r.mass_out = c->totals + 9;
   r.counter = c->counters + 1;
+  r.part = c->red_part;
   return r;
 }
 
@@ -485,7 +487,8 @@ int create_ctx(const wt_grid* grid, const wt_sim* sim, cudaStream_t ext, wt_ctx*
       (rc = dalloc(c, &c->mass_partial, (uint64_t)c->geom.nblocks * warps_per_block(c->geom) * 8)) ||
       (rc = dalloc(c, &c->hist, (uint64_t)WT_HIST_CAP * 16 * 8)) || (rc = dalloc(c, &c->totals, 18 * 8)) ||
       (rc = dalloc(c, &c->raw_totals, 12 * 4)) || (rc = dalloc(c, &c->counters, 4 * 4)) ||
-      (rc = dalloc(c, &c->hist_pos, 8)) || (rc = dalloc(c, &c->d_reduce, sizeof(ReduceArgs))))
+      (rc = dalloc(c, &c->hist_pos, 8)) || (rc = dalloc(c, &c->d_reduce, sizeof(ReduceArgs))) ||
+      (rc = dalloc(c, &c->red_part, WT_RED_PART * 8)))
     return cleanup(rc);
   if (cudaMemsetAsync(c->solid, 0, n, c->stream) != cudaSuccess || cudaMemsetAsync(c->emit, 0, n * 4, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->totals, 0, 18 * 8, c->stream) != cudaSuccess ||
@@ -523,7 +526,7 @@ int wt_destroy(wt_ctx* c) {
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
                   c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters,
-                  c->hist_pos, c->d_reduce, c->car_body, c->car_parts, c->car_rig};
+                  c->hist_pos, c->d_reduce, c->car_body, c->car_parts, c->car_rig, c->red_part};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);

@@ -20,6 +20,10 @@
 
 #define WT_HIST_CAP 16384u    // per-step force records kept on the device (ring)
 #define WT_PENDING_MAX 64u    // steps whose partials wait for one reduction launch
+#define WT_RED_FCHUNKS 8u     // blocks per step of the force reduction
+#define WT_RED_MCHUNKS 32u    // blocks of the mass reduction
+// scratch doubles per lattice for the reduction's chunk sums
+#define WT_RED_PART ((size_t)WT_PENDING_MAX * WT_RED_FCHUNKS * 16 + WT_RED_MCHUNKS)
 
 namespace wt {
 
@@ -106,6 +110,7 @@ struct ReduceArgs {
   uint32_t nmass;
   double* mass_out;
   unsigned int* counter;
+  double* part;  // WT_RED_PART doubles: chunk sums of the force records, then of the mass
 };
 cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t nsteps, bool with_mass,
                                 cudaStream_t s);

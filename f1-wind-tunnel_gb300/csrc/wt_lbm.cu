@@ -698,6 +698,7 @@ __global__ void coarse_average_kernel(const float4* __restrict__ fields, const u
 // into the history ring; block nsteps sums the mass partials; the last block to
 // finish folds the steps into the running totals in step order.
 constexpr uint32_t RED_THREADS = 256;
+constexpr uint32_t RED_FCHUNKS = WT_RED_FCHUNKS, RED_MCHUNKS = WT_RED_MCHUNKS;
 
 __device__ __forceinline__ double block_sum_d(double v, double* sm) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -712,6 +713,12 @@ __device__ __forceinline__ double block_sum_d(double v, double* sm) {
   return t;
 }
 
+// Pending steps' per-block force records into per-step history records and the
+// totals, and the per-warp mass partials into the mass.  Each step's records
+// are split into RED_FCHUNKS fixed ranges and the mass partials into
+// RED_MCHUNKS, one block each; the last block to finish combines the chunk sums
+// in chunk order.  The order of every sum is fixed, so the result is the same
+// on every run.
 __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceArgs* __restrict__ all, uint32_t nsteps,
                                                                    uint32_t with_mass) {
   __shared__ double sm[RED_THREADS / 32];
@@ -720,23 +727,27 @@ __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceA
   const ReduceArgs& ra = all[blockIdx.y];
   const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
   const uint64_t hist_base = *ra.hist_pos;
-  if (blockIdx.x < nsteps) {
-    const uint32_t step = blockIdx.x;
+  const uint32_t nforce = nsteps * RED_FCHUNKS;
+  double* const mpart = ra.part + (size_t)WT_PENDING_MAX * RED_FCHUNKS * 16;
+  if (blockIdx.x < nforce) {
+    const uint32_t step = blockIdx.x / RED_FCHUNKS, chunk = blockIdx.x % RED_FCHUNKS;
+    const uint32_t per = (ra.nslots + RED_FCHUNKS - 1) / RED_FCHUNKS;
+    const uint32_t s0 = chunk * per, s1 = min(s0 + per, ra.nslots);
     const ForceSlot* base = ra.slots + (size_t)step * ra.nslots;
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     uint32_t racc[6] = {0, 0, 0, 0, 0, 0};
-    for (uint32_t s = t; s < ra.nslots; s += RED_THREADS) {
+    for (uint32_t s = s0 + t; s < s1; s += RED_THREADS) {
       const ForceSlot r = base[s];
 #pragma unroll
       for (int k = 0; k < 9; k++) acc[k] += r.f[k];
 #pragma unroll
       for (int k = 0; k < 6; k++) racc[k] += (uint32_t)r.raw[k];
     }
-    double* rec = ra.hist + ((hist_base + step) % ra.hist_cap) * 16;
+    double* out = ra.part + (size_t)blockIdx.x * 16;
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       const double v = block_sum_d(acc[k], sm);
-      if (t == 0) rec[k] = v;
+      if (t == 0) out[k] = v;
     }
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1)
@@ -749,19 +760,44 @@ __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceA
       for (int k = 0; k < 6; k++) {
         uint32_t v = 0;
         for (uint32_t w = 0; w < RED_THREADS / 32; w++) v += smr[k][w];
-        rec[9 + k] = (double)(int32_t)v;
+        out[9 + k] = (double)v;  // exact: below 2^32
       }
   } else if (with_mass) {
+    const uint32_t chunk = blockIdx.x - nforce;
+    const uint32_t per = (ra.nmass + RED_MCHUNKS - 1) / RED_MCHUNKS;
+    const uint32_t s0 = chunk * per, s1 = min(s0 + per, ra.nmass);
     double acc = 0.0;
-    for (uint32_t s = t; s < ra.nmass; s += RED_THREADS) acc += ra.mass_partial[s];
+    for (uint32_t s = s0 + t; s < s1; s += RED_THREADS) acc += ra.mass_partial[s];
     const double v = block_sum_d(acc, sm);
-    if (t == 0) *ra.mass_out = v;
+    if (t == 0) mpart[chunk] = v;
   }
   __threadfence();
   if (t == 0) last = (atomicAdd(ra.counter, 1u) == gridDim.x - 1);
   __syncthreads();
-  if (last && t == 0) {
-    __threadfence();
+  if (!last) return;
+  __threadfence();
+  for (uint32_t i = t; i < nsteps * 16; i += RED_THREADS) {  // per-step records, chunks in order
+    const uint32_t step = i / 16, k = i % 16;
+    if (k >= 15) continue;
+    const double* in = ra.part + (size_t)step * RED_FCHUNKS * 16 + k;
+    double* rec = ra.hist + ((hist_base + step) % ra.hist_cap) * 16;
+    if (k < 9) {
+      double v = 0.0;
+      for (uint32_t c = 0; c < RED_FCHUNKS; c++) v += in[(size_t)c * 16];
+      rec[k] = v;
+    } else {
+      uint32_t v = 0;
+      for (uint32_t c = 0; c < RED_FCHUNKS; c++) v += (uint32_t)in[(size_t)c * 16];
+      rec[k] = (double)(int32_t)v;
+    }
+  }
+  if (with_mass && t == 0) {
+    double v = 0.0;
+    for (uint32_t c = 0; c < RED_MCHUNKS; c++) v += mpart[c];
+    *ra.mass_out = v;
+  }
+  __syncthreads();
+  if (t == 0) {
     for (uint32_t s = 0; s < nsteps; s++) {
       const double* r = ra.hist + ((hist_base + s) % ra.hist_cap) * 16;
       for (int k = 0; k < 9; k++) ra.totals[k] += r[k];
@@ -888,7 +924,8 @@ cudaError_t launch_batch_step(uint32_t storage, bool gather, bool write_fields, 
 cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t nsteps, bool with_mass,
                                 cudaStream_t s) {
   if ((nsteps == 0 && !with_mass) || count == 0) return cudaSuccess;
-  force_reduce_kernel<<<dim3(nsteps + 1, count), RED_THREADS, 0, s>>>(args, nsteps, with_mass ? 1u : 0u);
+  force_reduce_kernel<<<dim3(nsteps * RED_FCHUNKS + (with_mass ? RED_MCHUNKS : 0u), count), RED_THREADS, 0, s>>>(
+      args, nsteps, with_mass ? 1u : 0u);
   return cudaGetLastError();
 }
 
