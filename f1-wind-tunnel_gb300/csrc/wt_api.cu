@@ -72,6 +72,7 @@ struct wt_ctx {
   unsigned long long* hist_pos = nullptr;  // device: per-step records written so far
   ReduceArgs* d_reduce = nullptr;          // device: this lattice's reduction record
   double* red_part = nullptr;              // device: the reduction's chunk sums
+  float* heat_src = nullptr;               // device: the neighbours' largest emission per cell
   uint32_t bx = 128, by = 1;               // step-kernel block shape
   uint64_t version = 0;                    // bumped whenever kernel arguments change
   // Force records of steps not yet reduced (single-lattice path): the reduction
@@ -223,6 +224,7 @@ int flush_forces(wt_ctx* c);
 int rebuild_links(wt_ctx* c) {
   if (int rc = flush_forces(c)) return rc;  // pending records use the current slot layout
   WT_CUDA(c, launch_cell_words(c->solid, c->emit, c->cellw, c->nx, c->ny, c->nz, c->stream));
+  WT_CUDA(c, launch_heat_sources(c->emit, c->heat_src, c->nx, c->ny, c->nz, c->stream));
   uint8_t* dflags = nullptr;
   WT_CUDA(c, cudaMallocAsync((void**)&dflags, c->geom.nblocks, c->stream));
   WT_CUDA(c, launch_block_flags(c->cellw, c->geom, c->nx, c->ny, c->nz, dflags, c->stream));
@@ -301,7 +303,7 @@ StepArgs step_args(const wt_ctx* c) {
 
 cudaError_t enqueue_heat(wt_ctx* c, int heat_passes, float dt, cudaStream_t s) {
   HeatArgs h;
-  h.fields = c->fields; h.emit = c->emit;
+  h.fields = c->fields; h.emit = c->emit; h.src = c->heat_src;
   h.nx = c->nx; h.ny = c->ny; h.nz = c->nz;
   h.dt = dt;
   h.cool = c->sim.heat_cool; h.diffuse = c->sim.heat_diffuse; h.src_mix = c->sim.heat_src_mix;
@@ -488,9 +490,10 @@ int create_ctx(const wt_grid* grid, const wt_sim* sim, cudaStream_t ext, wt_ctx*
       (rc = dalloc(c, &c->hist, (uint64_t)WT_HIST_CAP * 16 * 8)) || (rc = dalloc(c, &c->totals, 18 * 8)) ||
       (rc = dalloc(c, &c->raw_totals, 12 * 4)) || (rc = dalloc(c, &c->counters, 4 * 4)) ||
       (rc = dalloc(c, &c->hist_pos, 8)) || (rc = dalloc(c, &c->d_reduce, sizeof(ReduceArgs))) ||
-      (rc = dalloc(c, &c->red_part, WT_RED_PART * 8)))
+      (rc = dalloc(c, &c->red_part, WT_RED_PART * 8)) || (rc = dalloc(c, &c->heat_src, n * 4)))
     return cleanup(rc);
   if (cudaMemsetAsync(c->solid, 0, n, c->stream) != cudaSuccess || cudaMemsetAsync(c->emit, 0, n * 4, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->heat_src, 0, n * 4, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->totals, 0, 18 * 8, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->raw_totals, 0, 48, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->counters, 0, 16, c->stream) != cudaSuccess ||
@@ -526,7 +529,7 @@ int wt_destroy(wt_ctx* c) {
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   void* bufs[] = {c->pop, c->cellw, c->solid, c->emit, c->fields, c->tA, c->tB, c->outlet_u, c->tau0_x,
                   c->block_slot, c->slots, c->mass_partial, c->hist, c->totals, c->raw_totals, c->counters,
-                  c->hist_pos, c->d_reduce, c->car_body, c->car_parts, c->car_rig, c->red_part};
+                  c->hist_pos, c->d_reduce, c->car_body, c->car_parts, c->car_rig, c->red_part, c->heat_src};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);

@@ -67,6 +67,7 @@ void fill_slot_offsets(StepArgs& a);
 struct HeatArgs {
   const float4* fields;
   const float* emit;
+  const float* src;  // the neighbours' largest emission (launch_heat_sources)
   const float* tin;
   float* tout;
   uint32_t nx, ny, nz;
@@ -151,6 +152,7 @@ cudaError_t launch_solid_from_u32(const uint32_t* in, uint8_t* solid, uint64_t n
 
 // wt_heat.cu
 cudaError_t launch_heat(const HeatArgs& a, cudaStream_t s);
+cudaError_t launch_heat_sources(const float* emit, float* src, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s);
 
 // wt_conv.cu: last error of the calling thread in the network operators (wt_net.h)
 std::string& net_error();
