@@ -797,15 +797,19 @@ __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceA
     *ra.mass_out = v;
   }
   __syncthreads();
+  // the totals: one thread per component, the steps in order
+  if (t < 9) {
+    double v = ra.totals[t];
+    for (uint32_t s = 0; s < nsteps; s++) v += ra.hist[((hist_base + s) % ra.hist_cap) * 16 + t];
+    ra.totals[t] = v;
+  } else if (t < 15) {
+    const uint32_t g = (t - 9) / 2, comp = (t - 9) % 2;  // raw x / y of group g
+    uint32_t v = (uint32_t)ra.raw_totals[3 * g + comp];
+    for (uint32_t s = 0; s < nsteps; s++)
+      v += (uint32_t)(int32_t)ra.hist[((hist_base + s) % ra.hist_cap) * 16 + 9 + 2 * g + comp];
+    ra.raw_totals[3 * g + comp] = (int32_t)v;
+  }
   if (t == 0) {
-    for (uint32_t s = 0; s < nsteps; s++) {
-      const double* r = ra.hist + ((hist_base + s) % ra.hist_cap) * 16;
-      for (int k = 0; k < 9; k++) ra.totals[k] += r[k];
-      for (int g = 0; g < 3; g++) {
-        ra.raw_totals[3 * g] = (int32_t)((uint32_t)ra.raw_totals[3 * g] + (uint32_t)(int32_t)r[9 + 2 * g]);
-        ra.raw_totals[3 * g + 1] = (int32_t)((uint32_t)ra.raw_totals[3 * g + 1] + (uint32_t)(int32_t)r[10 + 2 * g]);
-      }
-    }
     *ra.hist_pos = hist_base + nsteps;
     *ra.counter = 0u;
   }
