@@ -31,6 +31,10 @@ __device__ __forceinline__ int zmir(int z, int nz) {  // idx_of's z: mirror, the
 }
 
 __global__ void heat_kernel(HeatArgs a) {
+  // chained like the step kernels: the next launch may be scheduled now; wait
+  // for the fields and temperatures of the previous launch
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int nx = (int)a.nx, ny = (int)a.ny, nz = (int)a.nz;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -102,10 +106,16 @@ cudaError_t launch_heat_sources(const float* emit, float* src, uint32_t nx, uint
 }
 
 cudaError_t launch_heat(const HeatArgs& a, cudaStream_t s) {
-  const dim3 block(128, 1, 1);
-  const dim3 g((a.nx + 127) / 128, a.ny, a.nz);
-  heat_kernel<<<g, block, 0, s>>>(a);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((a.nx + 127) / 128, a.ny, a.nz);
+  cfg.blockDim = dim3(128, 1, 1);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;  // programmatic dependent launch
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, heat_kernel, a);
 }
 
 }  // namespace wt

@@ -721,6 +721,10 @@ __device__ __forceinline__ double block_sum_d(double v, double* sm) {
 // on every run.
 __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceArgs* __restrict__ all, uint32_t nsteps,
                                                                    uint32_t with_mass) {
+  // chained like the step kernels: the next launch may be scheduled now; wait
+  // for the steps whose records this reads
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   __shared__ double sm[RED_THREADS / 32];
   __shared__ uint32_t smr[6][RED_THREADS / 32];
   __shared__ bool last;
@@ -928,9 +932,8 @@ cudaError_t launch_batch_step(uint32_t storage, bool gather, bool write_fields, 
 cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t nsteps, bool with_mass,
                                 cudaStream_t s) {
   if ((nsteps == 0 && !with_mass) || count == 0) return cudaSuccess;
-  force_reduce_kernel<<<dim3(nsteps * RED_FCHUNKS + (with_mass ? RED_MCHUNKS : 0u), count), RED_THREADS, 0, s>>>(
-      args, nsteps, with_mass ? 1u : 0u);
-  return cudaGetLastError();
+  return launch_chained(force_reduce_kernel, dim3(nsteps * RED_FCHUNKS + (with_mass ? RED_MCHUNKS : 0u), count),
+                        dim3(RED_THREADS), s, args, nsteps, with_mass ? 1u : 0u);
 }
 
 // The force readout in one launch: the accumulators into a wt_forces record
@@ -938,6 +941,8 @@ cudaError_t launch_force_reduce(const ReduceArgs* args, uint32_t count, uint32_t
 // One warp; each lane reads its words before it clears them.
 __global__ void force_readback_kernel(double* totals, int32_t* raw, unsigned int* counters, wt_forces* out,
                                       uint64_t steps, int reset) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const uint32_t t = threadIdx.x;
   if (t < 9) {
     out->sum[t] = totals[t];
@@ -957,8 +962,7 @@ __global__ void force_readback_kernel(double* totals, int32_t* raw, unsigned int
 
 cudaError_t launch_force_readback(double* totals, int32_t* raw, unsigned int* counters, wt_forces* out,
                                   uint64_t steps, int reset, cudaStream_t s) {
-  force_readback_kernel<<<1, 32, 0, s>>>(totals, raw, counters, out, steps, reset);
-  return cudaGetLastError();
+  return launch_chained(force_readback_kernel, dim3(1), dim3(32), s, totals, raw, counters, out, steps, reset);
 }
 
 cudaError_t launch_read_pop(uint32_t storage, const void* pop, float* out, uint32_t n, uint64_t np, cudaStream_t s) {
