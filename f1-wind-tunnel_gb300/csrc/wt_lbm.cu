@@ -726,6 +726,7 @@ __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceA
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
   __shared__ double sm[RED_THREADS / 32];
+  __shared__ double smf[9][RED_THREADS / 32];
   __shared__ uint32_t smr[6][RED_THREADS / 32];
   __shared__ bool last;
   const ReduceArgs& ra = all[blockIdx.y];
@@ -748,24 +749,29 @@ __global__ void __launch_bounds__(RED_THREADS) force_reduce_kernel(const ReduceA
       for (int k = 0; k < 6; k++) racc[k] += (uint32_t)r.raw[k];
     }
     double* out = ra.part + (size_t)blockIdx.x * 16;
+    // the nine FP64 sums and six integer sums together: warp trees (as
+    // block_sum_d forms them), one barrier, then the warps in order
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
-      const double v = block_sum_d(acc[k], sm);
-      if (t == 0) out[k] = v;
-    }
+    for (int s = 16; s > 0; s >>= 1) {
 #pragma unroll
-    for (int s = 16; s > 0; s >>= 1)
+      for (int k = 0; k < 9; k++) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], s);
 #pragma unroll
       for (int k = 0; k < 6; k++) racc[k] += __shfl_down_sync(0xffffffffu, racc[k], s);
-    if (lane == 0)
+    }
+    if (lane == 0) {
+      for (int k = 0; k < 9; k++) smf[k][warp] = acc[k];
       for (int k = 0; k < 6; k++) smr[k][warp] = racc[k];
+    }
     __syncthreads();
-    if (t == 0)
-      for (int k = 0; k < 6; k++) {
-        uint32_t v = 0;
-        for (uint32_t w = 0; w < RED_THREADS / 32; w++) v += smr[k][w];
-        out[9 + k] = (double)v;  // exact: below 2^32
-      }
+    if (t < 9) {
+      double v = 0.0;
+      for (uint32_t w = 0; w < RED_THREADS / 32; w++) v += smf[t][w];
+      out[t] = v;
+    } else if (t < 15) {
+      uint32_t v = 0;
+      for (uint32_t w = 0; w < RED_THREADS / 32; w++) v += smr[t - 9][w];
+      out[t] = (double)v;  // exact: below 2^32
+    }
   } else if (with_mass) {
     const uint32_t chunk = blockIdx.x - nforce;
     const uint32_t per = (ra.nmass + RED_MCHUNKS - 1) / RED_MCHUNKS;
