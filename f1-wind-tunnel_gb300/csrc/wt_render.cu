@@ -45,11 +45,12 @@ __device__ __forceinline__ ushort4 pack(float r, float g, float b, float a) {
 }
 
 // One thread per pixel.
+template <bool MESH>
 __global__ void __launch_bounds__(64) scene_kernel(const Scene S, const SceneArgs a) {
   const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= a.w || y >= a.h) return;
-  const float4 c = render_pixel(S, a, x, y);
+  const float4 c = render_pixel<MESH>(S, a, x, y);
   a.scene[(size_t)y * a.w + x] = pack(c.x, c.y, c.z, c.w);
 }
 
@@ -394,7 +395,8 @@ dim3 tiles(uint32_t w, uint32_t h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h
 cudaError_t launch_render_scene(const SceneArgs& a, cudaStream_t s) {
   const Scene S = make_scene(a.shape, a.car);
   const dim3 b(8, 8);
-  scene_kernel<<<tiles(a.w, a.h, b), b, 0, s>>>(S, a);
+  if (a.mesh_mode != 0u) scene_kernel<true><<<tiles(a.w, a.h, b), b, 0, s>>>(S, a);
+  else scene_kernel<false><<<tiles(a.w, a.h, b), b, 0, s>>>(S, a);
   return cudaGetLastError();
 }
 

@@ -384,6 +384,10 @@ __device__ __noinline__ V3 shade_surface(const Scene& S, const SceneArgs& a, V3 
 }
 
 // RENDER fs_main (render-wgsl.ts:288-398) for pixel (x, y): colour and hit distance.
+// MESH: look.meshMode != 0 (a separate instantiation, so the analytic scenes'
+// kernel carries none of the G-buffer code: the pass is bound by instruction
+// supply).
+template <bool MESH>
 __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, uint32_t y) {
   const float ux = ((float)x + 0.5f) / (float)a.w, uy = ((float)y + 0.5f) / (float)a.h;
   const float ndx = (ux * 2.0f - 1.0f) + a.jitter_x, ndy = (1.0f - uy * 2.0f) + a.jitter_y;
@@ -395,7 +399,7 @@ __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, u
   float t_hit = FAR;
   V2 hit = v2(FAR, 0.0f);
   float4 gn = make_float4(0.0f, 0.0f, 0.0f, 0.0f), ga = gn, gm = gn;
-  if (a.mesh_mode != 0u) {
+  if constexpr (MESH) {
     // the G-buffer texel under the pixel (it has the scene's size)
     const int gx0 = to_i32(ux * (float)a.w), gy0 = to_i32(uy * (float)a.h);
     const int gx = gx0 < 0 ? 0 : (gx0 > (int)a.w - 1 ? (int)a.w - 1 : gx0);
@@ -419,7 +423,7 @@ __device__ float4 render_pixel(const Scene& S, const SceneArgs& a, uint32_t x, u
     const float vd = hit.x;
     V3 n;
     Mat mt;
-    if (a.mesh_mode != 0u) {
+    if constexpr (MESH) {
       n = nrm3(v3(gn.x, gn.y, gn.z));
       if (dot3(n, rd) > 0.0f) n = -n;
       const V3 alb = v3(ga.x, ga.y, ga.z);

@@ -118,7 +118,7 @@ void wthm_render(const void* shape, const void* cam_p, const void* look_p, const
   const Scene S = make_scene(a.shape, g_car);
   for (uint32_t y = y0; y < y1 && y < hgt; y++)
     for (uint32_t x = 0; x < w; x++) {
-      const float4 c = render_pixel(S, a, x, y);
+      const float4 c = a.mesh_mode != 0u ? render_pixel<true>(S, a, x, y) : render_pixel<false>(S, a, x, y);
       float* o = out + ((size_t)y * w + x) * 4;
       o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
     }
