@@ -448,7 +448,7 @@ __device__ __noinline__ float sd_w17_part(const Scene& S, V3 pb, uint32_t part) 
   return sample3(S.car.parts, (int)S.car.pdims[0], (int)S.car.pdims[1], (int)S.car.pdims[2], uvw) * mn(sc, 1.0f);
 }
 // sdW17 (f1.ts:354-369)
-__device__ V2 sd_w17(const Scene& S, V3 pw) {
+__device__ __noinline__ V2 sd_w17(const Scene& S, V3 pw) {
   const V3 pa = v3(pw.x, pw.y, ab(pw.z));
   const V3 p = w17_body_frame(S, pa);
   const float squeeze = 1.0f - rig_at(S.car.rig, RIG_EXTRA).z * pod_weight(p);
