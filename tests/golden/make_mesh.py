@@ -81,6 +81,7 @@ def edge_mesh():
     q_b = quad((-0.5, -0.8, 2.0), (1.0, -0.8, 2.0), (1.0, 0.5, 2.0), (-0.5, 0.5, 2.0))
     d_a = quad((-0.8, -0.3, 2.0), (0.3, -0.3, 2.0), (0.3, 0.6, 2.0), (-0.8, 0.6, 2.0))
     d_b = quad((-0.3, -0.6, 2.0), (0.8, -0.6, 2.0), (0.8, 0.3, 2.0), (-0.3, 0.3, 2.0))
+    cutout = quad((0.3, 0.12, 1.2), (0.8, 0.12, 1.2), (0.8, 0.42, 1.2), (0.3, 0.42, 1.2))
     b = len(v)
     v += [[0.2, 0.2, 1.0, 0, 0, 0, -1, 0], [0.4, 0.4, 1.0, 1, 0, 0, -1, 0], [0.6, 0.6, 1.0, 0, 0, 0, -1, 1]]
     degenerate = [b, b + 1, b + 2]
@@ -91,7 +92,7 @@ def edge_mesh():
     v += [[-0.6, -0.6, -0.5, 0, 0, 0, -1, 0], [0.6, -0.4, 3.0, 1, 0, 0, -1, 0], [0.1, 0.7, 3.0, 0, 0, 0, -1, 1]]
     crossing = [b, b + 1, b + 2]
     groups = [("wall", wall), ("quad_a", q_a), ("quad_b", q_b + degenerate + behind), ("crossing", crossing + [0]),
-              ("decal_a", d_a), ("decal_b", d_b)]
+              ("cutout", cutout), ("decal_a", d_a), ("decal_b", d_b)]
     idx, ranges = [], {}
     for name, ii in groups:
         ranges[name] = (len(idx), len(ii))
@@ -107,6 +108,9 @@ def edge_mesh():
         DrawSpec("empty", (1.0, 1.0, 1.0, 1.0), alpha_cut=0.0, first=0, count=0, **m),
         DrawSpec("quad_b", (0.1, 0.9, 0.1, 1.0), alpha_cut=0.0, first=ranges["quad_b"][0], count=12, **m),
         DrawSpec("crossing", (0.1, 0.1, 0.9, 1.0), alpha_cut=0.0, first=ranges["crossing"][0], count=4, **m),
+        # an opaque draw with an alpha cut (MeshCar never makes one; the pipeline allows it): the
+        # texture's alpha ramp cuts it, and the cut fragments neither write nor hide the wall
+        DrawSpec("cutout", (0.9, 0.8, 0.2, 1.0), alpha_cut=0.5, first=ranges["cutout"][0], count=6, texture=0, **m),
         DrawSpec("decal_a", (1.0, 1.0, 1.0, 0.7), alpha_cut=0.02, first=ranges["decal_a"][0], count=6, texture=0,
                  blend=True, **m),
         DrawSpec("decal_b", (0.2, 0.4, 1.0, 0.6), alpha_cut=0.02, first=ranges["decal_b"][0], count=6, blend=True, **m),
