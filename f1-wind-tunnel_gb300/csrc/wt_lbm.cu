@@ -569,7 +569,7 @@ cudaError_t launch_chained(K kernel, dim3 grid, dim3 block, cudaStream_t s, Args
 }
 
 template <class St, bool GATHER, bool FIELDS>
-__global__ void __launch_bounds__(256, St::min_blocks) step_kernel(StepArgs a) {
+__global__ void __maxnreg__(St::max_regs) step_kernel(StepArgs a) {
   chain_enter();
   step_tile<St, GATHER, FIELDS>(a, OfsTable{a}, a.slots, blockIdx, make_uint3(gridDim.x, gridDim.y, gridDim.z));
 }
@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(256, St::min_blocks) step_kernel(StepArgs a) {
 // Many lattices in one launch: block b belongs to the lattice L with
 // tile_base[L] <= b < tile_base[L+1]; its coordinates follow that lattice's grid.
 template <class St, bool GATHER, bool FIELDS>
-__global__ void __launch_bounds__(256, St::min_blocks) batch_step_kernel(const StepArgs* __restrict__ args,
+__global__ void __maxnreg__(St::max_regs) batch_step_kernel(const StepArgs* __restrict__ args,
                                                             const BatchTiles* __restrict__ tiles, uint32_t count,
                                                             uint32_t pending) {
   chain_enter();
