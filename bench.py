@@ -313,6 +313,20 @@ def run_render(args, rank, world):
     eng.set_shape(shape_p)
     eng.reset()
     cam = orbit({}, W / H)
+    if args.profile:
+        # whole engine frames only, few launches before them (for ncu captures):
+        # 8 LBM steps, heat, the streamline pass and the render passes per frame
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            viewer.frame(cam, 8)
+        eng.sync()
+        if rank == 0:
+            print(json.dumps({"profile_frames": args.steps, "s": time.perf_counter() - t0}), flush=True)
+        if mesh is not None:
+            mesh.close()
+        viewer.close()
+        eng.close()
+        return
     for _ in range(40):                       # develop the flow
         viewer.frame(cam, 8)
     view = viewer.view_uniform()
@@ -433,6 +447,9 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=64, help="LBM steps per kernel-timing launch batch")
+    ap.add_argument("--kernel-seconds", type=float, default=1.5,
+                    help="device time of the kernel-only timing region (clocks are sampled through it)")
+    ap.add_argument("--e2e-frames", type=int, default=4000, help="at most this many end-to-end frames (~1.5 s)")
     ap.add_argument("--no-tune", action="store_true", help="skip the block-shape autotuner")
     ap.add_argument("--profile", action="store_true",
                     help="warm-up and timed frames only (for ncu captures); prints a short line")
@@ -507,14 +524,17 @@ def main():
     eng.read_forces_raw()
     barrier()
 
-    # ---- timed device region: K frames, inputs resident in HBM
+    # ---- timed device region: K frames, inputs resident in HBM.  The clock
+    # sampler stays on through the kernel-only region below, which runs for at
+    # least --kernel-seconds of device time, so the clock record holds several
+    # samples under load even when K frames take only milliseconds.
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0)
-        e1.record(stream)
-        barrier()
+    clk = ClockSampler(local).__enter__()
+    e0.record(stream)
+    for _ in range(args.steps):
+        eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0)
+    e1.record(stream)
+    barrier()
     ms = e0.elapsed_time(e1)
     ms = max_over_ranks(ms)
     frames = args.steps
@@ -522,6 +542,7 @@ def main():
     value = total_cells * lbm_per_frame * frames / (ms / 1e3) / 1e6
     fr = eng.read_forces_raw()
     if args.profile:
+        clk.__exit__(None, None, None)
         if rank == 0:
             print(json.dumps({"profile_frames": frames, "ms": ms, "mlups": value}), flush=True)
         eng.close()
@@ -533,18 +554,28 @@ def main():
     # per frame: the step kernels and two heat passes; one force reduction per 64 steps
     launches_timed = args.steps * (lbm_per_frame + 2) + (args.steps * lbm_per_frame) // 64
 
-    # ---- the collide-stream kernel alone: batches of kernel_steps steps, no heat
+    # ---- the collide-stream kernel alone: batches of kernel_steps steps, no heat,
+    # repeated for at least --kernel-seconds of device time
     ks = max(2, args.kernel_steps - args.kernel_steps % 2)
-    reps = max(2, 512 // ks)
     eng.step(ks, 0)
     barrier()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(4):
+        eng.step(ks, 0)
+    p1.record(stream)
+    barrier()
+    est = p0.elapsed_time(p1) / 4 / 1e3  # seconds per batch
+    reps = max(8, int(args.kernel_seconds / max(est, 1e-6)) + 1)
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record(stream)
     for _ in range(reps):
         eng.step(ks, 0)
     k1.record(stream)
     barrier()
-    kms = k0.elapsed_time(k1) / (reps * ks)  # per LBM step (one reduction launch per ks steps included)
+    clk.__exit__(None, None, None)
+    kernel_region_ms = k0.elapsed_time(k1)
+    kms = kernel_region_ms / (reps * ks)  # per LBM step (one reduction launch per ks steps included)
     bpl = bytes_per_lup(args.storage)
     achieved = n * bpl / (kms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
@@ -553,7 +584,8 @@ def main():
     # Every frame's forces come back to the host, read asynchronously like the
     # reference's mapped readback (engine.ts:746-760): frame k's copy is collected
     # while frame k+1 runs, and the last one before the clock stops.
-    e2e_frames = max(5, min(args.steps, 100))
+    # about a second and a half of frames (at most --e2e-frames), so its host clock is not noise
+    e2e_frames = max(5, min(args.e2e_frames, int(1500.0 / max(ms / frames, 1e-3))))
     barrier()
     t0 = time.perf_counter()
     prev = None
@@ -593,11 +625,14 @@ def main():
                 "traffic": profiled_traffic(args.storage), "peak_source": peak_kind,
                 "kernel": "collide-stream step", "algorithmic_bytes_per_lup": bpl,
                 "kernel_ms_per_step": kms, "kernel_mlups": n / (kms / 1e3) / 1e6,
+                "kernel_steps_timed": reps * ks, "kernel_region_ms": kernel_region_ms,
             },
             "cpu_baseline": base,
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches_timed,
-            "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+            "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"],
+                       "samples": clocks["samples"],
+                       "window": "the timed frames and the kernel-only region that follows them"},
         }
         print(json.dumps(line), flush=True)
     eng.close()

@@ -23,6 +23,19 @@ using namespace wt;
 
 struct wt_renderer;
 struct wt_mesh;
+
+// Largest float t with sqrt_rn(t) <= 0.35f: sqrt_rn(x) > 0.35f <=> x > t (correctly
+// rounded sqrt is monotonic), so the kernel can test u.u without a square root.
+float wt::guard_threshold() {
+  static float t = [] {
+    float x = 0.35f * 0.35f;
+    while (__builtin_sqrtf(x) > 0.35f) x = __builtin_nextafterf(x, 0.0f);
+    while (__builtin_sqrtf(__builtin_nextafterf(x, 1.0f)) <= 0.35f) x = __builtin_nextafterf(x, 1.0f);
+    return x;
+  }();
+  return t;
+}
+
 namespace {
 void release_renderer_buffers(wt_renderer* r);
 void release_mesh_buffers(wt_mesh* m);
@@ -269,17 +282,6 @@ int rebuild_links(wt_ctx* c) {
   return WT_OK;
 }
 
-// Largest float t with sqrt_rn(t) <= 0.35f: sqrt_rn(x) > 0.35f <=> x > t (correctly
-// rounded sqrt is monotonic), so the kernel can test u.u without a square root.
-float guard_threshold() {
-  static float t = [] {
-    float x = 0.35f * 0.35f;
-    while (__builtin_sqrtf(x) > 0.35f) x = __builtin_nextafterf(x, 0.0f);
-    while (__builtin_sqrtf(__builtin_nextafterf(x, 1.0f)) <= 0.35f) x = __builtin_nextafterf(x, 1.0f);
-    return x;
-  }();
-  return t;
-}
 
 uint32_t warps_per_block(const StepGeom& g) { return (g.block.x * g.block.y + 31) / 32; }
 

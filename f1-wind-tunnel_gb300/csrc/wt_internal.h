@@ -63,6 +63,9 @@ struct StepArgs {
 
 // Fills own_ofs / pull_ofs / push_ofs from nx, ny, np.
 void fill_slot_offsets(StepArgs& a);
+// The divergence guard's bound on u.u: the largest float whose square root
+// rounds to <= 0.35f (length(u) > 0.35, src/engine/wgsl.ts:238).
+float guard_threshold();
 
 struct HeatArgs {
   const float4* fields;

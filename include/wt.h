@@ -500,25 +500,35 @@ const char* wt_version(void);
  * allocator or memory budget (or share the lattice through graphics interop
  * memory) and so cannot create a wt_ctx, and code that must not hit the device
  * synchronisation cudaMalloc can cause in the middle of a frame.
- *   f      device, 19*n floats: post-collision populations in the reference's
- *          order f[i*n + idx] (what wt_read_populations returns)
- *   solid  device, n u32 flags (0 fluid, 1..3 groups);  emit: device, n floats
- *          (negative marks a duct cell whose links carry no force), or NULL
- *   out    host; out->sum / out->raw get the force the next collide-stream step
- *          takes from this state (as wt_read_force_history / wt_read_forces
- *          report it), out->steps = 1, the other fields 0.
- * Scratch is a static device array of WT_NOALLOC_BLOCKS + 1 records (98,400 B)
- * that every GPU loading the library holds until exit; its address is looked
- * up on the first call on each device, so make that first call before any
- * stream capture.  All calls share it: calls that overlap on the GPU race.
+ *   f       device, 19*n floats: post-collision populations in the reference's
+ *           order f[i*n + idx] (what wt_read_populations returns)
+ *   solid   device, n u32 flags (0 fluid, 1..3 groups)
+ *   emit    device, n floats (negative marks a duct cell whose links carry no
+ *           force), or NULL
+ *   fields  device, n x (ux, uy, uz, rho) floats of the previous step (what
+ *           wt_read_fields returns); only the outlet column x = nx-1 is read,
+ *           for its outflow equilibrium.  NULL takes (u_in, 0, 0) there.
+ *   u_in    inlet speed (wt_sim.u_in): inlet and far-field equilibria, belt speed
+ *   out     host; out->sum / out->raw get the force the next collide-stream step
+ *           takes from this state, as wt_read_force_history / wt_read_forces
+ *           report it: the same boundary precedence, and cells whose moments
+ *           trip the divergence guard contribute nothing (their count is in
+ *           out->guarded); out->steps = 1, out->mass = 0.
+ * Scratch is a static device array of WT_NOALLOC_BLOCKS + 2 records
+ * (98,496 B) that every GPU loading the library holds until exit.  Its device
+ * address is looked up on the first call on each device and kept for the
+ * process, which assumes the device's primary context is not reset
+ * (cudaDeviceReset) between calls.  All calls share the array: calls that
+ * overlap on the GPU race.  Every call synchronises `stream` (a cudaStream_t,
+ * NULL = legacy default stream) before returning, so it cannot be recorded
+ * into a CUDA graph: a stream under capture is refused with WT_ERR_ARG.
  * Lattices above WT_NOALLOC_MAX_CELLS cells are rejected with
- * WT_ERR_NOALLOC_LIMIT.  Synchronises `stream` (a cudaStream_t, NULL = legacy
- * default stream) before returning. */
+ * WT_ERR_NOALLOC_LIMIT, lattices below 8x3x3 with WT_ERR_ARG. */
 #define WT_NOALLOC_BLOCKS 1024u
 #define WT_NOALLOC_MAX_CELLS 134217728ull /* 2^27 */
 #define WT_ERR_NOALLOC_LIMIT (-7)
-int wt_forces_noalloc(const float* f, const uint32_t* solid, const float* emit, uint32_t nx, uint32_t ny,
-                      uint32_t nz, void* stream, wt_forces* out);
+int wt_forces_noalloc(const float* f, const uint32_t* solid, const float* emit, const float* fields, uint32_t nx,
+                      uint32_t ny, uint32_t nz, float u_in, void* stream, wt_forces* out);
 
 #ifdef __cplusplus
 }

@@ -11,6 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libwgslref.so")
 REF_SRC = os.path.join(HERE, "_ref", "wgsl_modules.inc")
+# the reference checkout the translator reads (only where it is present)
+REFERENCE_ROOT = os.environ.get("WT_REFERENCE_ROOT", "/root/reference")
 _vp = ctypes.c_void_p
 _F = ctypes.c_float
 
@@ -22,7 +24,7 @@ def build_oracle():
 
 def build_ref():
     """Compile the translated reference if its generated source is present."""
-    if os.path.exists(REF_SRC) or os.path.isdir("/root/reference"):
+    if os.path.exists(REF_SRC) or os.path.isdir(REFERENCE_ROOT):
         r = subprocess.run(["make", "-s", "-C", HERE, "ref"], capture_output=True, text=True)
         return os.path.exists(REF_SO) and r.returncode == 0
     return False

@@ -201,7 +201,7 @@ def test_png_decode_every_filter(wt_lib):
 
 
 def test_w17_assets_build_the_mesh(wt_lib):
-    assets = "/root/reference/public/models"
+    assets = os.path.join(os.environ.get("WT_REFERENCE_ROOT", "/root/reference"), "public", "models")
     if not os.path.isdir(assets):
         pytest.skip("the reference's W17 assets are not on this machine")
     import json

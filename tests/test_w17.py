@@ -17,7 +17,7 @@ from conftest import ROOT
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 sys.path.insert(0, GOLDEN)
-ASSETS = "/root/reference/public/models"
+ASSETS = os.path.join(os.environ.get("WT_REFERENCE_ROOT", "/root/reference"), "public", "models")
 SYNTH_SHA = {"A": "5390fb17dac47e42a20a694c765c5665eaca3c51bbf33918300e89d06c4a716f",
              "B": "7152e927ed4d76525904bd8385e188808f4cd0cf6bc06cd4231ee02202c18ae6"}
 
