@@ -19,6 +19,7 @@
 // with tcgen05.ld (warp w owns lanes 32w..32w+31).  Every mbarrier wait is
 // bounded: on expiry the kernel raises g_conv_error, still waits (bounded) for
 // its own MMAs, frees its tensor memory and returns.
+#include <atomic>
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -56,7 +57,13 @@ struct GemmArgs {
   const float* bias;
   void* out;               // FWD bf16 y[M][cout], DGRAD f32 dx[M][cin], WGRAD f32 ws[split][M][N]
   int relu;
+  uint32_t stage_wait;     // polls of a K-slice stage wait (WAIT_LIMIT unless a test lowers it)
 };
+
+// Poll budget of the pipeline's stage waits for the next launches (see
+// wt_net_set_stage_wait_limit); the drain before tensor memory is freed always
+// uses WAIT_LIMIT.
+std::atomic<uint32_t> g_stage_wait{WAIT_LIMIT};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -81,8 +88,8 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; i++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -241,7 +248,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) conv_gemm_kernel(GemmArgs p) {
   for (uint32_t kt = 0; kt < nk; kt++) {
     const uint32_t s = kt & 1u;
     bool w = true;
-    if (kt >= 2) w = mbar_wait(smem_u32(&bars[s]), ((kt >> 1) - 1) & 1u);  // MMAs of slice kt-2 done
+    if (kt >= 2) w = mbar_wait(smem_u32(&bars[s]), ((kt >> 1) - 1) & 1u, p.stage_wait);  // MMAs of slice kt-2 done
     if (!__syncthreads_and(w)) {  // the block stops together
       ok = false;
       break;
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) conv_gemm_kernel(GemmArgs p) {
   // All MMAs done: the last commit covers every earlier one of the issuing thread.
   if (issued > 0) {
     const uint32_t last = issued - 1;
-    const bool done = mbar_wait(smem_u32(&bars[last & 1u]), (last >> 1) & 1u);
+    const bool done = mbar_wait(smem_u32(&bars[last & 1u]), (last >> 1) & 1u, WAIT_LIMIT);
     ok = ok && done;
   }
   if (!ok && t == 0) atomicExch(&g_conv_error, 1);
@@ -382,6 +389,7 @@ GemmArgs base_args(const wt_conv_shape* s) {
   GemmArgs p = {};
   p.batch = s->batch; p.d = s->d; p.h = s->h; p.w = s->w;
   p.cin = s->cin; p.cout = s->cout; p.taps = s->taps;
+  p.stage_wait = g_stage_wait.load();
   return p;
 }
 
@@ -467,5 +475,7 @@ int wt_net_check(void) {
 }
 
 const char* wt_net_last_error(void) { return net_error().c_str(); }
+
+uint32_t wt_net_set_stage_wait_limit(uint32_t polls) { return g_stage_wait.exchange(polls); }
 
 }  // extern "C"

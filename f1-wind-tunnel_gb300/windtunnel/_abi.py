@@ -183,6 +183,8 @@ _PROTOS = {
     "wt_read_fields": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "wt_read_populations": (ctypes.c_int, [_vp, _vp]),
     "wt_write_state": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "wt_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "wt_load": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "wt_reset_from": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]),
     "wt_info_get": (ctypes.c_int, [_vp, ctypes.POINTER(Info)]),
     "wt_stream": (_vp, [_vp]),

@@ -15,6 +15,7 @@ Rendering, particles and streamlines of frame() are not part of this path.
 """
 import ctypes
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -336,6 +337,14 @@ class AeroEngine:
         ua, up = ptr(fields, np.float32, 4 * self.n)
         ta, tp = ptr(temps, np.float32, self.n)
         self._check(self.lib.wt_write_state(self.ctx, fp, up, tp), "wt_write_state")
+
+    def save(self, path):
+        """Checkpoint the whole simulation state to a file (wt_save)."""
+        self._check(self.lib.wt_save(self.ctx, os.fsencode(path)), "wt_save")
+
+    def load(self, path):
+        """Resume from a checkpoint of a lattice of the same size and storage (wt_load)."""
+        self._check(self.lib.wt_load(self.ctx, os.fsencode(path)), "wt_load")
 
     def reset_from(self, coarse_u_rho):
         c = np.ascontiguousarray(coarse_u_rho, dtype=np.float32)

@@ -33,6 +33,7 @@ PROTOS = {
     "wt_nn_adam": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _u64, _f, _f, _f, _f, _u32, _vp]),
     "wt_nn_to_bf16": (ctypes.c_int, [_vp, _vp, _u64, _vp]),
     "wt_net_check": (ctypes.c_int, []),
+    "wt_net_set_stage_wait_limit": (ctypes.c_uint32, [ctypes.c_uint32]),
     "wt_net_last_error": (ctypes.c_char_p, []),
 }
 

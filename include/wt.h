@@ -39,6 +39,7 @@ extern "C" {
 #define WT_ERR_UNSUPPORTED (-4) /* scene kind or option not built */
 #define WT_ERR_STATE (-5)       /* call not valid in the current state */
 #define WT_ERR_DEVICE (-6)      /* no sm_103a device / wrong architecture */
+#define WT_ERR_IO (-8)          /* checkpoint file not writable / readable, damaged or of another build */
 
 /* Population storage format (see wt_sim.storage). */
 #define WT_STORE_F32 0u  /* f_i as float: 19*4 B per cell */
@@ -203,6 +204,21 @@ int wt_read_populations(wt_ctx* ctx, float* f);
 /* Replace the state: populations f[19n] (post-collision, reference order),
  * optional u_rho[4n] (fields, also the outlet's previous velocity) and temps[n]. */
 int wt_write_state(wt_ctx* ctx, const float* f, const float* u_rho, const float* temps);
+
+/* Checkpoint and resume (no reference counterpart: the reference keeps its state
+ * only in GPU buffers, src/engine/engine.ts:234-260).  wt_save writes the whole
+ * simulation state to `path`: populations in the storage format's own bits,
+ * solid flags, emission, temperatures, fields, the outlet column's velocities,
+ * the force readout accumulators, the step counters, the simulation parameters
+ * and the voxelized shape, with a checksum.  wt_load restores it into a context
+ * of the same lattice size and storage format (WT_ERR_ARG otherwise); the run
+ * then continues bit for bit as if it had not stopped.  Not stored: the
+ * per-step force history (wt_read_force_history sees only steps after the load),
+ * the block shape, and the W17 model (voxel flags are stored; re-voxelizing a W17
+ * shape after a load needs wt_set_car_model).  Damaged, truncated or foreign
+ * files give WT_ERR_IO; a failed load may leave the context partly overwritten. */
+int wt_save(wt_ctx* ctx, const char* path);
+int wt_load(wt_ctx* ctx, const char* path);
 
 /* Warm start: set populations to feq(rho, u) of a coarse (ux,uy,uz,rho) field
  * u_rho[4*cx*cy*cz] trilinearly resampled to the lattice; fields likewise. */

@@ -81,6 +81,15 @@ int wt_nn_to_bf16(const float* x, void* y, uint64_t n, void* stream);
 int wt_net_check(void);
 const char* wt_net_last_error(void);
 
+/* Fault-path test hook: the number of polls each K-slice stage wait of the
+ * convolution pipeline makes before it gives up (default 2^21), for the
+ * launches that follow; returns the previous value.  0 makes every stage wait
+ * give up at once, so a convolution with more than two K slices leaves its K
+ * loop, reports the expiry through wt_net_check and writes no output.  The
+ * wait for the issued MMAs before tensor memory is freed always keeps its full
+ * limit.  Not for production use; restore the returned value afterwards. */
+uint32_t wt_net_set_stage_wait_limit(uint32_t polls);
+
 #ifdef __cplusplus
 }
 #endif

@@ -169,3 +169,32 @@ def test_mse_and_adam(ops, ref):
         pw = pw - 1e-2 * (mw / (1 - 0.9 ** k)) / (np.sqrt(vw / (1 - 0.999 ** k)) + 1e-8)
     assert np.allclose(p.cpu().numpy(), pw, rtol=1e-5, atol=1e-6)
     assert np.array_equal(pb.float().cpu().numpy(), ref.bf16_round(p.cpu().numpy()))
+
+
+def test_stage_wait_expiry_is_reported(ops, ref):
+    """The pipeline's bounded stage wait made to run out (a poll budget of 0):
+    every block leaves its K loop at the third slice, waits with the full limit
+    for the MMAs it issued, frees its tensor memory and raises the flag that
+    wt_net_check reports; the output is left unwritten.  The next launch with the
+    normal budget succeeds and matches the oracle."""
+    from windtunnel import WindTunnelError
+    rng = np.random.default_rng(5)
+    b, d, h, w, cin, cout, taps = 1, 6, 6, 8, 16, 32, 27  # K = 432: 7 K slices
+    x = rand(rng, (b, d, h, w, cin))
+    wt = rand(rng, (cout, taps, cin), 1.0 / np.sqrt(taps * cin))
+    xs, ws = bf16_tensor(x), bf16_tensor(wt)
+    y = torch.full((b, d, h, w, cout), 7.0, dtype=torch.bfloat16, device="cuda")
+    ops.check()
+    prev = ops.lib.wt_net_set_stage_wait_limit(0)
+    try:
+        ops.conv_forward(xs, ws, None, y, False)
+        with pytest.raises(WindTunnelError, match="wait expired"):
+            ops.check()
+    finally:
+        ops.lib.wt_net_set_stage_wait_limit(prev)
+    assert bool((y.float() == 7.0).all())  # no block wrote a partial result
+    ops.conv_forward(xs, ws, None, y, False)
+    ops.check()
+    want = ref.conv3d(x, wt)
+    got = y.float().cpu().numpy().astype(np.float64)
+    assert np.all(np.abs(got - want) <= 2.0 ** -8 * np.abs(want) + 1e-4 * np.abs(want).max())
