@@ -186,6 +186,12 @@ StepArgs step_args(const wt_ctx* c) {
   memcpy(a.feq_in, c->feq_in, sizeof(a.feq_in));
   memcpy(a.floor_k, c->floor_k, sizeof(a.floor_k));
   memcpy(a.feq_guard, c->feq_guard, sizeof(a.feq_guard));
+  const float S = c->sim.storage == WT_STORE_F16 ? 16384.0f : 1.0f;  // f16 keeps (f - w) 2^14, bf16 f - w
+  for (int i = 0; i < 19; i++) {
+    a.dev_in[i] = (c->feq_in[i] - Wd(i)) * S;
+    a.floor_kd[i] = c->floor_k[i] * S;
+    a.dev_guard[i] = (c->feq_guard[i] - Wd(i)) * S;
+  }
   a.guard_uu = guard_threshold();
   fill_slot_offsets(a);
   a.prefetch_ahead = c->prefetch_ahead;

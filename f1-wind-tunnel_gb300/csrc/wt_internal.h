@@ -53,6 +53,9 @@ struct StepArgs {
   float feq_in[19];            // feq(i, 1, (u_in, 0, 0))
   float floor_k[19];           // 6 * w_i * c_ix (belt term coefficient)
   float feq_guard[19];         // feq(i, 1, (u_in/2, 0, 0)): the divergence guard's reset state
+  // the same three tables as scaled deviations S (f - w_i) for f16 / bf16 storage
+  // (S = 2^14 / 1), the step's working form there
+  float dev_in[19], floor_kd[19], dev_guard[19];
   // Slot offsets relative to the cell index, modulo 2^32 (19 * np < 2^32):
   uint32_t own_ofs[19];        // i * np:                  pop[i][x]
   uint32_t pull_ofs[19];       // opp(i) * np - off(c_i):  pop[opp(i)][x - c_i]

@@ -93,6 +93,10 @@ struct StoreF16 {
   __device__ __forceinline__ static void st(T* p, float v, float w) {
     *p = __float2half_rn(__fmaf_rn(v, F16_SCALE, -(w * F16_SCALE)));
   }
+  // the stored deviation itself, in units of 2^-14 (the step kernel's working form)
+  static constexpr float S = F16_SCALE;
+  __device__ __forceinline__ static float ldd(const T* p) { return __half2float(__ldg(p)); }
+  __device__ __forceinline__ static void std_(T* p, float d) { *p = __float2half_rn(d); }
 };
 struct StoreBF16 {
   typedef __nv_bfloat16 T;
@@ -102,6 +106,9 @@ struct StoreBF16 {
   __device__ __forceinline__ static float ld(const T* p, float w) { return w + __bfloat162float(__ldg(p)); }
   __device__ __forceinline__ static float ld_smem(const T* p, float w) { return w + __bfloat162float(*p); }
   __device__ __forceinline__ static void st(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
+  static constexpr float S = 1.0f;
+  __device__ __forceinline__ static float ldd(const T* p) { return __bfloat162float(__ldg(p)); }
+  __device__ __forceinline__ static void std_(T* p, float d) { *p = __float2bfloat16_rn(d); }
 };
 
 }  // namespace wt

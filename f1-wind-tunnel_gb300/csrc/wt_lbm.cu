@@ -116,7 +116,8 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
     rcp = 1.0f;
     ux = u_in * 0.5f; uy = 0.0f; uz = 0.0f;
   }
-  sfor<19>([&](auto I) { g[I] = guard ? feq_guard[I] : f[I]; });
+  sfor<19>([&](auto I) { g[I] = f[I]; });
+  if (guard) sfor<19>([&](auto I) { g[I] = feq_guard[I]; });
   if (duct) {
     const float t = 0.04f, tu = 1.0f - 0.04f;
     ux = ux * tu + (0.55f * u_in) * t;
@@ -127,19 +128,11 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
   const float uu15 = 1.5f * uu;
   const float wr0 = Wd(0) * rho, wr1 = Wd(1) * rho, wr2 = Wd(7) * rho;
   float eq[19];
-  // Opposite directions share 3 c.u (exact negation) and 4.5 (c.u)^2 (identical bits).
-  eq[0] = wr0 * (1.0f + 3.0f * 0.0f + 4.5f * 0.0f * 0.0f - uu15);
-  sfor<9>([&](auto P) {
-    constexpr int i = 2 * P + 1;  // odd member of the pair (i, i + 1)
-    const float cu = cdot<i>(ux, uy, uz);
-    const float t3 = 3.0f * cu;
-    const float t45 = 4.5f * cu * cu;
-    const float wr = (i < 7 ? wr1 : wr2);
-    eq[i] = wr * (1.0f + t3 + t45 - uu15);
-    eq[i + 1] = wr * (1.0f - t3 + t45 - uu15);
-  });
   float pxx = 0.0f, pyy = 0.0f, pzz = 0.0f, pxy = 0.0f, pxz = 0.0f, pyz = 0.0f;
-  sfor<19>([&](auto I) {
+  // Pi^neq accumulated as each equilibrium is formed, directions in order 0..18
+  // (every sum keeps the reference's order), so each incoming population dies
+  // as soon as its term is taken.
+  auto acc = [&](auto I) {
     constexpr int i = I;
     constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
     const float ne = g[i] - eq[i];
@@ -152,6 +145,20 @@ __device__ __forceinline__ CellOut collide(const float (&f)[19], float (&fo)[19]
     if constexpr (cx * cz < 0) pxz = pxz - ne;
     if constexpr (cy * cz > 0) pyz = pyz + ne;
     if constexpr (cy * cz < 0) pyz = pyz - ne;
+  };
+  // Opposite directions share 3 c.u (exact negation) and 4.5 (c.u)^2 (identical bits).
+  eq[0] = wr0 * (1.0f + 3.0f * 0.0f + 4.5f * 0.0f * 0.0f - uu15);
+  acc(std::integral_constant<int, 0>{});
+  sfor<9>([&](auto P) {
+    constexpr int i = 2 * P + 1;  // odd member of the pair (i, i + 1)
+    const float cu = cdot<i>(ux, uy, uz);
+    const float t3 = 3.0f * cu;
+    const float t45 = 4.5f * cu * cu;
+    const float wr = (i < 7 ? wr1 : wr2);
+    eq[i] = wr * (1.0f + t3 + t45 - uu15);
+    eq[i + 1] = wr * (1.0f - t3 + t45 - uu15);
+    acc(std::integral_constant<int, i>{});
+    acc(std::integral_constant<int, i + 1>{});
   });
   const float q = __fsqrt_rn(pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
   // ks2 q / rho with rho in [0.3, 3] (or 1 after the guard) and rcp = RN(1/rho):
@@ -196,11 +203,149 @@ __device__ __forceinline__ void stp(void* pop, int dir, uint32_t np, uint32_t ce
   St::st(reinterpret_cast<typename St::T*>(pop) + (size_t)dir * np + cell, v, Wd(wdir));
 }
 
+// Regularized + Smagorinsky collision (wgsl.ts:231-272) on scaled deviations
+// d_i = S (f_i - w_i), the step's working form for f16 / bf16 storage: the same
+// model written out on moments, in FP32 with fused multiply-adds and the
+// hardware's approximate reciprocal and square root.  It does not keep the
+// reference's operation order (the f32 path's collide() does, bit for bit); its
+// accuracy is judged against the FP64 oracle by the precision tests.
+//   rho = 1 + dr, dr = sum d / S;  j = sum c d / S;  u = j / rho
+//   Pi^neq_ab = sum c_a c_b d / S - rho u_a u_b - dr delta_ab / 3
+//     (sum_i w_i c_ia c_ib = delta_ab / 3; the equilibrium's second moment is
+//      rho u_a u_b + rho delta_ab / 3)
+//   f_i' - w_i = w_i (dr - 1.5 rho u.u + rho (3 c.u + 4.5 (c.u)^2)) + 4.5 (1 - 1/tau) w_i (c_i c_i - I/3):Pi^neq
+// Directions pair as (i, opp i) for odd i: sums s and differences m of each pair
+// give the moments; pairs 0 x, 1 y, 2 z, 3 (+x+y), 4 (+x-y), 5 (+x+z), 6 (+x-z),
+// 7 (+y+z), 8 (+y-z), named by their odd member.
+template <class St>
+__device__ __forceinline__ CellOut collide_dev(const float (&d)[19], float (&fo)[19], float tau0, float u_in, float ks2,
+                                               bool duct, float guard_uu) {
+  constexpr float S = St::S, iS = 1.0f / St::S;
+  CellOut o;
+  float s[9], m[9];
+  sfor<9>([&](auto P) {
+    constexpr int i = 2 * P + 1;
+    s[P] = d[i] + d[i + 1];
+    m[P] = d[i] - d[i + 1];
+  });
+  const float sd = ((d[0] + s[0]) + (s[1] + s[2])) + (((s[3] + s[4]) + (s[5] + s[6])) + (s[7] + s[8]));
+  const float jx = ((m[0] + m[3]) + (m[4] + m[5])) + m[6];
+  const float jy = ((m[1] + m[3]) - m[4]) + (m[7] + m[8]);
+  const float jz = ((m[2] + m[5]) - m[6]) + (m[7] - m[8]);
+  float sxx = ((s[0] + s[3]) + (s[4] + s[5])) + s[6];
+  float syy = ((s[1] + s[3]) + (s[4] + s[7])) + s[8];
+  float szz = ((s[2] + s[5]) + (s[6] + s[7])) + s[8];
+  float sxy = s[3] - s[4], sxz = s[5] - s[6], syz = s[7] - s[8];
+  float dr = sd * iS;
+  float rho = 1.0f + dr;
+  float rr = __fdividef(1.0f, rho);
+  const float q = rr * iS;
+  float ux = jx * q, uy = jy * q, uz = jz * q;
+  // divergence guard (wgsl.ts:238-243): non-finite, rho outside [0.3, 3] or |u| > 0.35
+  const float uu0 = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+  const bool guard = !(rho >= 0.3f && rho <= 3.0f && uu0 <= guard_uu);
+  if (guard) {  // f = feq(1, (u_in/2, 0, 0)): its deviation moments are u_a u_b (scaled)
+    rho = 1.0f;
+    dr = 0.0f;
+    rr = 1.0f;
+    ux = u_in * 0.5f;
+    uy = 0.0f;
+    uz = 0.0f;
+    sxx = S * ux * ux;
+    syy = szz = sxy = sxz = syz = 0.0f;
+  }
+  if (duct) {  // wgsl.ts:248
+    const float t = 0.04f, tu = 1.0f - 0.04f;
+    ux = ux * tu + (0.55f * u_in) * t;
+    uy = uy * tu + uy * t;
+    uz = uz * tu + uz * t;
+  }
+  const float uu = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+  const float rux = rho * ux, ruy = rho * uy, ruz = rho * uz;
+  const float dr3 = dr * (1.0f / 3.0f);
+  const float pxx = fmaf(sxx, iS, -fmaf(rux, ux, dr3));
+  const float pyy = fmaf(syy, iS, -fmaf(ruy, uy, dr3));
+  const float pzz = fmaf(szz, iS, -fmaf(ruz, uz, dr3));
+  const float pxy = fmaf(sxy, iS, -(rux * uy));
+  const float pxz = fmaf(sxz, iS, -(rux * uz));
+  const float pyz = fmaf(syz, iS, -(ruy * uz));
+  const float q2 = fmaf(pxx, pxx, fmaf(pyy, pyy, pzz * pzz)) + 2.0f * fmaf(pxy, pxy, fmaf(pxz, pxz, pyz * pyz));
+  const float qn = q2 * rsqrtf(fmaxf(q2, 1e-30f));  // sqrt(q2), 0 for q2 = 0
+  const float arg = fmaf(tau0, tau0, ks2 * qn * rr);
+  const float tau = 0.5f * (tau0 + arg * rsqrtf(arg));  // arg >= tau0^2 > 0
+  const float k = fmaf(-4.5f, __fdividef(1.0f, tau), 4.5f);
+  const float tr3 = ((pxx + pyy) + pzz) * (1.0f / 3.0f);
+  const float a = fmaf(-1.5f * rho, uu, dr);
+  const float r3 = 3.0f * rho, r45 = 4.5f * rho;
+  const float qx = pxx - tr3, qy = pyy - tr3, qz = pzz - tr3;
+  const float bxy = qx + pyy, bxz = qx + pzz, byz = qy + pzz;
+  const float qd[9] = {qx, qy, qz, fmaf(2.0f, pxy, bxy), fmaf(-2.0f, pxy, bxy), fmaf(2.0f, pxz, bxz),
+                       fmaf(-2.0f, pxz, bxz), fmaf(2.0f, pyz, byz), fmaf(-2.0f, pyz, byz)};
+  fo[0] = (S * Wd(0)) * fmaf(-k, tr3, a);
+  sfor<9>([&](auto P) {
+    constexpr int i = 2 * P + 1;
+    const float cu = cdot<i>(ux, uy, uz);
+    const float e = fmaf(r45 * cu, cu, fmaf(k, qd[P], a));
+    constexpr float W = S * Wd(i);
+    const float ew = W * e;
+    const float lin = r3 * cu;
+    fo[i] = fmaf(W, lin, ew);
+    fo[i + 1] = fmaf(-W, lin, ew);
+  });
+  o.ux = ux; o.uy = uy; o.uz = uz; o.rho = rho; o.guard = guard;
+  return o;
+}
+
+// How the step holds a cell's populations in registers: absolute f_i for f32
+// storage (with the reference's arithmetic in collide(), bit for bit), scaled
+// deviations d_i = S (f_i - w_i) for f16 / bf16 storage (their stored form,
+// collided by collide_dev).  Boundary values come in the same form.
+template <class St>
+struct Rep {
+  typedef typename St::T T;
+  static constexpr bool dev = false;
+  __device__ __forceinline__ static float ld(const T* p, int dir) { return St::ld(p, Wd(dir)); }
+  __device__ __forceinline__ static void st(T* p, float v, int dir) { St::st(p, v, Wd(dir)); }
+  __device__ __forceinline__ static float solid(int k) { return Wd(k); }  // wgsl.ts:183
+  __device__ __forceinline__ static float feq_in(const StepArgs& a, int i) { return a.feq_in[i]; }
+  __device__ __forceinline__ static float floor_k(const StepArgs& a, int i) { return a.floor_k[i]; }
+  template <int i> __device__ __forceinline__ static float outlet(float ux, float uy, float uz) {
+    return feq_rho1<i>(ux, uy, uz);
+  }
+  template <int i> __device__ __forceinline__ static float link_t(float v) { return 2.0f * (v - Wd(i)); }
+};
+template <class St>
+struct RepDev {
+  typedef typename St::T T;
+  static constexpr bool dev = true;
+  __device__ __forceinline__ static float ld(const T* p, int) { return St::ldd(p); }
+  __device__ __forceinline__ static void st(T* p, float v, int) { St::std_(p, v); }
+  __device__ __forceinline__ static float solid(int) { return 0.0f; }
+  __device__ __forceinline__ static float feq_in(const StepArgs& a, int i) { return a.dev_in[i]; }
+  __device__ __forceinline__ static float floor_k(const StepArgs& a, int i) { return a.floor_kd[i]; }
+  template <int i> __device__ __forceinline__ static float outlet(float ux, float uy, float uz) {
+    return (feq_rho1<i>(ux, uy, uz) - Wd(i)) * St::S;
+  }
+  template <int i> __device__ __forceinline__ static float link_t(float v) { return v * (2.0f / St::S); }
+};
+template <> struct Rep<StoreF16> : RepDev<StoreF16> {};
+template <> struct Rep<StoreBF16> : RepDev<StoreBF16> {};
+
+// A population of direction dir at cell index `cell` in the step's form.
+template <class St>
+__device__ __forceinline__ float ldr(const void* pop, int dir, uint32_t np, uint32_t cell) {
+  return Rep<St>::ld(reinterpret_cast<const typename St::T*>(pop) + (size_t)dir * np + cell, dir);
+}
+template <class St>
+__device__ __forceinline__ void str(void* pop, int dir, uint32_t np, uint32_t cell, float v, int wdir) {
+  Rep<St>::st(reinterpret_cast<typename St::T*>(pop) + (size_t)dir * np + cell, v, wdir);
+}
+
 // Momentum exchange of one force-carrying link (wgsl.ts:221-223): the bounced
 // value v = f[i]; group from the source cell's solid flag.
-template <int i>
+template <int i, class R>
 __device__ __forceinline__ void link_force(float v, uint32_t group, float (&gf)[9]) {
-  const float t = 2.0f * (v - Wd(i));
+  const float t = R::template link_t<i>(v);
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     if (group == (uint32_t)(k + 1)) {
@@ -296,6 +441,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
   const uint32_t idx = in ? x + nx * y + nxy * z : 0u;
   const uint32_t cw = in ? __ldg(a.cellw + idx) : CW_SOLID;
   typedef typename St::T PT;
+  typedef Rep<St> R;
   PT* __restrict__ P = reinterpret_cast<PT*>(a.pop);
   float gf[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   float rho_cell = 0.0f;
@@ -317,8 +463,8 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
 
   if (in && (cw & CW_SOLID)) {
     if constexpr (!GATHER) {  // wgsl.ts:183: solid cells hold w_i
-      if constexpr (Ofs::plain_path) sfor<19>([&](auto K) { St::st(ofs.template own_at<K>(P, idx), Wd(K), Wd(K)); });
-      else sfor<19>([&](auto K) { stp<St>(a.pop, K, np, idx, Wd(K), K); });
+      if constexpr (Ofs::plain_path) sfor<19>([&](auto K) { R::st(ofs.template own_at<K>(P, idx), R::solid(K), K); });
+      else sfor<19>([&](auto K) { str<St>(a.pop, K, np, idx, R::solid(K), K); });
     }
     if constexpr (FIELDS) a.fields[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
   } else if (in) {
@@ -331,23 +477,23 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
     if (plain) {
       sfor<19>([&](auto I) {
         constexpr int i = I;
-        if constexpr (GATHER) f[i] = St::ld(P + (idx + ofs.template pull<i>()), Wd(i));
-        else f[i] = St::ld(ofs.template own_at<i>(P, idx), Wd(i));
+        if constexpr (GATHER) f[i] = R::ld(P + (idx + ofs.template pull<i>()), i);
+        else f[i] = R::ld(ofs.template own_at<i>(P, idx), i);
       });
     } else if (!yzface) {
       sfor<19>([&](auto I) {
         constexpr int i = I;
         if constexpr (i == 0) {
-          f[0] = ldp<St>(a.pop, 0, np, idx);
+          f[0] = ldr<St>(a.pop, 0, np, idx);
         } else if constexpr (GATHER) {
           constexpr int off_x = CXd(i), off_y = CYd(i), off_z = CZd(i);
           const int off = off_x + off_y * (int)nx + off_z * (int)nxy;
           const bool bb = (cw >> i) & 1u;
           const uint32_t slot = bb ? (uint32_t)i * np + idx : (uint32_t)OPPd(i) * np + (uint32_t)((int)idx - off);
           const int wdir = bb ? i : OPPd(i);
-          f[i] = St::ld(reinterpret_cast<const typename St::T*>(a.pop) + slot, Wd(wdir));
+          f[i] = R::ld(reinterpret_cast<const typename St::T*>(a.pop) + slot, wdir);
         } else {
-          f[i] = ldp<St>(a.pop, i, np, idx);
+          f[i] = ldr<St>(a.pop, i, np, idx);
         }
       });
     } else {
@@ -355,29 +501,29 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
         constexpr int i = I;
         constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
         if constexpr (i == 0) {
-          f[0] = ldp<St>(a.pop, 0, np, idx);
+          f[0] = ldr<St>(a.pop, 0, np, idx);
         } else {
           float v;
           if (cx > 0 && x == 0) {
-            v = a.feq_in[i];
+            v = R::feq_in(a, i);
           } else if (cx < 0 && x == nx - 1) {
-            v = feq_rho1<i>(pu.x, pu.y, pu.z);
+            v = R::template outlet<i>(pu.x, pu.y, pu.z);
           } else if (cy > 0 && y == 0) {
-            v = ldp<St>(a.pop, i, np, idx);
-            if constexpr (cx != 0) v = v + a.floor_k[i] * floor_u;
+            v = ldr<St>(a.pop, i, np, idx);
+            if constexpr (cx != 0) v = v + R::floor_k(a, i) * floor_u;
           } else if ((cy < 0 && y == ny - 1) || (cz < 0 && z == nz - 1)) {
-            v = a.feq_in[i];
+            v = R::feq_in(a, i);
           } else if (GATHER) {
             if ((cw >> i) & 1u) {
-              v = ldp<St>(a.pop, i, np, idx);
+              v = ldr<St>(a.pop, i, np, idx);
             } else if (cz > 0 && z == 0) {
-              v = ldp<St>(a.pop, OPPd(ZMIRd(i)), np, (uint32_t)((int)idx - cx - cy * (int)nx));
+              v = ldr<St>(a.pop, OPPd(ZMIRd(i)), np, (uint32_t)((int)idx - cx - cy * (int)nx));
             } else {
               const int off = cx + cy * (int)nx + cz * (int)nxy;
-              v = ldp<St>(a.pop, OPPd(i), np, (uint32_t)((int)idx - off));
+              v = ldr<St>(a.pop, OPPd(i), np, (uint32_t)((int)idx - off));
             }
           } else {
-            v = ldp<St>(a.pop, i, np, idx);
+            v = ldr<St>(a.pop, i, np, idx);
           }
           f[i] = v;
         }
@@ -386,14 +532,14 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
     if (!yzface) {  // inlet / outlet directions of the x-face lanes (wgsl.ts:207-210)
       if (x == 0) {
         sfor<19>([&](auto I) {
-          if constexpr (CXd(I) > 0) f[I] = a.feq_in[I];
+          if constexpr (CXd(I) > 0) f[I] = R::feq_in(a, I);
         });
       }
       if ((x | 31u) >= nx - 1) {  // warp-uniform: this warp holds the outlet column
         sfor<19>([&](auto I) {
           constexpr int i = I;
           if constexpr (CXd(i) < 0) {
-            const float e = feq_rho1<i>(pu.x, pu.y, pu.z);
+            const float e = R::template outlet<i>(pu.x, pu.y, pu.z);
             f[i] = (x == nx - 1) ? e : f[i];
           }
         });
@@ -410,14 +556,18 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
           if (((cw >> i) & 1u) && !mirrored) {
             const int off = cx + cy * (int)nx + cz * (int)nxy;
             const uint32_t grp = __ldg(solid_u8 + (uint32_t)((int)idx - off));
-            link_force<i>(f[i], grp, gf);
+            link_force<i, R>(f[i], grp, gf);
           }
         }
       });
     }
 
     // ---------------------------------------------------------------- collide
-    const CellOut o = collide(f, fo, __ldg(a.tau0_x + x), a.u_in, a.ks2, (cw & CW_DUCT) != 0, a.feq_guard, a.guard_uu);
+    CellOut o;
+    if constexpr (R::dev)
+      o = collide_dev<St>(f, fo, __ldg(a.tau0_x + x), a.u_in, a.ks2, (cw & CW_DUCT) != 0, a.guard_uu);
+    else
+      o = collide(f, fo, __ldg(a.tau0_x + x), a.u_in, a.ks2, (cw & CW_DUCT) != 0, a.feq_guard, a.guard_uu);
     if (o.guard) {
 #pragma unroll
       for (int k = 0; k < 9; k++) gf[k] = 0.0f;
@@ -431,25 +581,25 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
     if constexpr (!GATHER) {
       sfor<19>([&](auto J) {
         constexpr int j = J;
-        if constexpr (Ofs::plain_path) St::st(ofs.template own_at<OPPd(j)>(P, idx), fo[j], Wd(j));
-        else stp<St>(a.pop, OPPd(j), np, idx, fo[j], j);
+        if constexpr (Ofs::plain_path) R::st(ofs.template own_at<OPPd(j)>(P, idx), fo[j], j);
+        else str<St>(a.pop, OPPd(j), np, idx, fo[j], j);
       });
     } else if (plain) {
       sfor<19>([&](auto J) {
         constexpr int j = J;
-        St::st(P + (idx + ofs.template push<j>()), fo[j], Wd(j));
+        R::st(P + (idx + ofs.template push<j>()), fo[j], j);
       });
     } else if (!yzface) {
       sfor<19>([&](auto J) {
         constexpr int j = J;
         if constexpr (j == 0) {
-          stp<St>(a.pop, 0, np, idx, fo[0], 0);
+          str<St>(a.pop, 0, np, idx, fo[0], 0);
         } else {
           constexpr int i = OPPd(j);
           const int off = CXd(j) + CYd(j) * (int)nx + CZd(j) * (int)nxy;
           const bool bb = (cw >> i) & 1u;
           const uint32_t slot = bb ? (uint32_t)i * np + idx : (uint32_t)j * np + (uint32_t)((int)idx + off);
-          St::st(reinterpret_cast<typename St::T*>(a.pop) + slot, fo[j], Wd(j));
+          R::st(reinterpret_cast<typename St::T*>(a.pop) + slot, fo[j], j);
         }
       });
     } else {
@@ -458,23 +608,23 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
         constexpr int cx = CXd(j), cy = CYd(j), cz = CZd(j);
         constexpr int i = OPPd(j);
         if constexpr (j == 0) {
-          stp<St>(a.pop, 0, np, idx, fo[0], 0);
+          str<St>(a.pop, 0, np, idx, fo[0], 0);
         } else {
           if (cx < 0 && x == 0) {
             // inlet side: the reference never reads this value
           } else if (cx > 0 && x == nx - 1) {
             // outlet side: discarded
           } else if (cy < 0 && y == 0) {
-            stp<St>(a.pop, i, np, idx, fo[j], j);  // moving-floor bounce-back source
+            str<St>(a.pop, i, np, idx, fo[j], j);  // moving-floor bounce-back source
           } else if ((cy > 0 && y == ny - 1) || (cz > 0 && z == nz - 1)) {
             // far field: discarded
           } else if ((cw >> i) & 1u) {
-            stp<St>(a.pop, i, np, idx, fo[j], j);  // bounce-back source (mirror included)
+            str<St>(a.pop, i, np, idx, fo[j], j);  // bounce-back source (mirror included)
           } else if (cz < 0 && z == 0) {
-            stp<St>(a.pop, ZMIRd(j), np, (uint32_t)((int)idx + cx + cy * (int)nx), fo[j], j);
+            str<St>(a.pop, ZMIRd(j), np, (uint32_t)((int)idx + cx + cy * (int)nx), fo[j], j);
           } else {
             const int off = cx + cy * (int)nx + cz * (int)nxy;
-            stp<St>(a.pop, j, np, (uint32_t)((int)idx + off), fo[j], j);
+            str<St>(a.pop, j, np, (uint32_t)((int)idx + off), fo[j], j);
           }
         }
       });
