@@ -219,6 +219,31 @@ def run_aeromap(args, rank, world, dist):
     b.close()
 
 
+def run_aeromap_converge(args, rank, world):
+    """The aero-map metric: seconds until all 33 cases' windowed Cd and Cl are
+    within 1 % of their long-run FP32 values (windtunnel.studies.convergence_times):
+    plain FP32 cold one case after another, batched FP32 cold, batched FP32 and
+    FP16 warm-started.  value = the batched FP16 warm-started time (the north
+    star's method); the other three are in `times`."""
+    from windtunnel import studies
+    cases, labels = studies.sweep_cases(False)
+    model = studies.load_model(os.path.join(PKG, "windtunnel", "data", "warmstart_f1.npz"))
+    res = studies.convergence_times(cases, labels, args.horizon, model, log_fn=lambda m: None)
+    if args.record:
+        with open(args.record, "w") as f:
+            json.dump(res, f, indent=1)
+    if rank == 0:
+        sec = res["seconds"]
+        print(json.dumps({
+            "metric": "aeromap_seconds_to_1pct", "value": sec["batched_fp16_warm"], "unit": "s", "n_gpus": world,
+            "steps": args.horizon, "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f16", "data": "synthetic",
+            "config": {"workload": f"aero map: 25 ride-height cases 256x96x80 + 8 uneven lattices, horizon "
+                                   f"{args.horizon} steps, 1 % of the cold FP32 long-run Cd/Cl over 5760-step windows"},
+            "times": sec, "speedup_vs_plain": res["speedup_vs_plain"], "not_converged": res["not_converged"]}),
+              flush=True)
+
+
 def surrogate_flops(batch, d, h, w):
     """Multiply-add FLOPs (2 per MAC) of one training step's convolutions: forward,
     data gradient (not for the first layer) and weight gradient of every layer."""
@@ -439,8 +464,10 @@ def main():
     ap.add_argument("--steps", type=int, default=200, help="timed frames")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="wt", choices=["wt", "reference"])
-    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "surrogate", "render",
-                                                              "render-w17"])
+    ap.add_argument("--workload", default="f1", choices=["f1", "cube", "f1-512", "aeromap", "aeromap-converge",
+                                                              "surrogate", "render", "render-w17"])
+    ap.add_argument("--horizon", type=int, default=150000, help="aeromap-converge: LBM steps per case")
+    ap.add_argument("--record", default=None, help="aeromap-converge: write the full JSON record here")
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-frames", type=int, default=64, help="CPU-baseline frames (stops at 20 s)")
@@ -489,6 +516,11 @@ def main():
         return
     if args.workload in ("render", "render-w17"):
         run_render(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload == "aeromap-converge":
+        run_aeromap_converge(args, rank, world)
         if dist:
             dist.destroy_process_group()
         return

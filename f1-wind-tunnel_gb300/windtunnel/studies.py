@@ -6,10 +6,11 @@
         save the weights.
     python -m windtunnel.studies evaluate --weights FILE [--small] --out DIR
         warm vs cold FP32 starts of held-out seeds, evaluated by the LBM.
-    python -m windtunnel.studies sweep --weights FILE [--small] --out DIR
+    python -m windtunnel.studies sweep --weights FILE [--small] [--eval-steps N] --out DIR
         the 25-point ride-height aero map plus 8 uneven lattices: time to 1 %
         convergence of every case's windowed Cd and Cl, plain FP32 cold start
-        one case after another vs batched FP16 with the warm start.
+        one case after another vs batched FP32 cold, batched FP32 and FP16
+        warm-started (bench.py --workload aeromap-converge prints the same).
 """
 import argparse
 import json
@@ -21,6 +22,7 @@ import numpy as np
 
 from . import warmstart as ws
 from .surrogate import Surrogate
+from .warmstart import run_cases
 from .workloads import aeromap_cases
 
 
@@ -174,45 +176,65 @@ def sweep_cases(small=False):
     return [(d, h, shape) for d, _, h, shape, _ in cases], [lab for *_, lab in cases]
 
 
-def study_sweep(args):
-    """Time to 1 % convergence of all aero-map cases: plain FP32 cold start one case
-    after another (single-lattice launches) vs batched FP16 with the warm start."""
-    os.makedirs(args.out, exist_ok=True)
-    cases, labels = sweep_cases(args.small)
-    horizon = 4000 if args.small else args.eval_steps
-    model = load_model(args.weights)
-    log(f"{len(cases)} cases, horizon {horizon} steps")
-    # cold FP32 reference runs (batched for the study's own speed; the sequential
-    # cost of the plain path is its measured single-lattice step time x steps)
-    cold = ws.run_cases(cases, horizon, storage="f32")
+def convergence_times(cases, labels, horizon, model, log_fn=log):
+    """Seconds to 1 % convergence of every aero-map case (trailing 5760-step means
+    of Cd and Cl within 1 % of the case's long-run value from its cold FP32 run,
+    and staying there to the horizon), for four ways of running the map:
+      plain FP32 cold, one case after another (single-lattice launches);
+      batched FP32 cold; batched FP32 warm-started; batched FP16 warm-started.
+    The batched FP32 run is bit-identical to the single-lattice one (same
+    trajectories), so the plain path's time is every case's convergence step
+    times its measured single-lattice step time; a batch takes as long as its
+    slowest case.  A case that never converges counts the horizon (and is
+    reported)."""
+    cold = run_cases(cases, horizon, storage="f32")
     refs = [ws.reference_values(cold["cd"][i], cold["cl"][i]) for i in range(len(cases))]
-    cold_steps = [ws.convergence_step(cold["cd"][i], cold["cl"][i], *refs[i]) for i in range(len(cases))]
-    # single-lattice FP32 step time of every case size (plain path: one lattice at a time)
+
+    def steps_of(run):
+        return [ws.convergence_step(run["cd"][i], run["cl"][i], *refs[i]) for i in range(len(cases))]
+
+    cold_steps = steps_of(cold)
     t_single = {}
     for d, h, sh in cases:
         if d not in t_single:
             t_single[d] = single_lattice_step_s(d, h, sh)
-    # warm start: inference, then all cases batched in FP16
     t0 = time.time()
     fields = warm_fields(model, [sh for _, _, sh in cases])
     t_infer = time.time() - t0
-    warm = ws.run_cases(cases, horizon, warm=fields, storage="f16")
-    warm_steps = [ws.convergence_step(warm["cd"][i], warm["cl"][i], *refs[i]) for i in range(len(cases))]
-    # cold FP16 batched without the warm start (isolates the two effects)
-    coldb = ws.run_cases(cases, horizon, storage="f16")
-    coldb_steps = [ws.convergence_step(coldb["cd"][i], coldb["cl"][i], *refs[i]) for i in range(len(cases))]
+    warm32 = run_cases(cases, horizon, warm=fields, storage="f32")
+    warm16 = run_cases(cases, horizon, warm=fields, storage="f16")
+    w32, w16 = steps_of(warm32), steps_of(warm16)
     H = horizon
+
+    def last(steps):
+        return max((s if s is not None else H) for s in steps)
+
     plain_s = sum((c if c is not None else H) * t_single[d] for c, (d, _, _) in zip(cold_steps, cases))
-    batch_step = warm["group_step_s"][0]
-    warm_s = max((w if w is not None else H) for w in warm_steps) * batch_step + t_infer
-    coldb_s = max((w if w is not None else H) for w in coldb_steps) * coldb["group_step_s"][0]
-    res = {"cases": labels, "horizon": H, "cold_fp32_steps": cold_steps, "warm_fp16_batched_steps": warm_steps,
-           "cold_fp16_batched_steps": coldb_steps, "single_lattice_step_s": {str(k): v for k, v in t_single.items()},
-           "batched_fp16_step_s": batch_step, "inference_s": t_infer,
-           "plain_fp32_sequential_s": plain_s, "batched_fp16_cold_s": coldb_s, "batched_fp16_warm_s": warm_s,
-           "speedup_batched_warm": plain_s / warm_s, "speedup_batched_cold": plain_s / coldb_s,
+    res = {"cases": labels, "horizon": H, "window": ws.WINDOW, "tolerance": ws.TOLERANCE,
+           "cold_fp32_steps": cold_steps, "warm_fp32_batched_steps": w32, "warm_fp16_batched_steps": w16,
+           "not_converged": {"cold_fp32": sum(c is None for c in cold_steps), "warm_fp32": sum(c is None for c in w32),
+                             "warm_fp16": sum(c is None for c in w16)},
+           "single_lattice_step_s": {"x".join(map(str, k)): v for k, v in t_single.items()},
+           "batched_fp32_step_s": cold["group_step_s"][0], "batched_fp16_step_s": warm16["group_step_s"][0],
+           "inference_s": t_infer,
+           "seconds": {"plain_fp32_cold_sequential": plain_s,
+                       "batched_fp32_cold": last(cold_steps) * cold["group_step_s"][0],
+                       "batched_fp32_warm": last(w32) * warm32["group_step_s"][0] + t_infer,
+                       "batched_fp16_warm": last(w16) * warm16["group_step_s"][0] + t_infer},
            "refs": refs}
-    log(json.dumps({k: v for k, v in res.items() if k not in ("cases", "refs")}))
+    res["speedup_vs_plain"] = {k: plain_s / v for k, v in res["seconds"].items()}
+    log_fn(json.dumps({k: v for k, v in res.items() if k not in ("cases", "refs", "cold_fp32_steps",
+                                                              "warm_fp32_batched_steps", "warm_fp16_batched_steps")}))
+    return res
+
+
+def study_sweep(args):
+    """Time to 1 % convergence of all aero-map cases, four ways (convergence_times)."""
+    os.makedirs(args.out, exist_ok=True)
+    cases, labels = sweep_cases(args.small)
+    horizon = 4000 if args.small else args.eval_steps
+    log(f"{len(cases)} cases, horizon {horizon} steps")
+    res = convergence_times(cases, labels, horizon, load_model(args.weights))
     with open(os.path.join(args.out, "sweep_study.json"), "w") as f:
         json.dump(res, f, indent=1)
 

@@ -1,13 +1,20 @@
-"""Generate tests/golden/precision_fp64_128x48x40.json: the FP64 oracle's force
-history of the precision case (generic F1, seed 5, 128x48x40 cells at 9 cm,
-u_in 0.08, tau0 0.51, Cs 0.1, sponge 16), 20000 steps, for an ensemble of
-members that differ only by a 1e-5 perturbation of the initial populations
-(member 0 unperturbed).  The unsteady wake turns any difference of arithmetic
-into a different trajectory after a few thousand steps; the spread of the
-members' window means is the noise against which the stored formats are
-judged (tests/test_gpu_precision_study.py).
+"""Generate the FP64 oracle fixtures of the precision case (generic F1, seed 5,
+128x48x40 cells at 9 cm, u_in 0.08, Cs 0.1, sponge 16):
 
-    python tests/golden/make_precision.py [--members 4]
+  precision_fp64_128x48x40.json         tau0 0.51 (the benchmark's value), 20000
+      steps, an ensemble of members that differ only by a 1e-5 perturbation of
+      the initial populations (member 0 unperturbed).  The unsteady wake turns
+      any difference of arithmetic into a different trajectory after a few
+      hundred steps and the case has several long-lived states; the spread of
+      the members' window means is the noise against which the stored formats'
+      statistics are judged.
+  precision_fp64_steady_128x48x40.json  tau0 0.6, 8000 steps, one run: the same
+      car in steady flow, where window means are deterministic and a 1 %
+      bound on Cd and Cl is decidable.
+
+Both hold per-200-step block force means (tests/test_gpu_precision_study.py).
+
+    python tests/golden/make_precision.py [--members 4] [--steady]
 
 Test infrastructure: runs the oracle (oracle/pyoracle.py), minutes per member."""
 import argparse
@@ -28,11 +35,17 @@ DIMS, H, SEED = (128, 48, 40), 0.09, 5
 STEPS, BLOCK = 20000, 200
 PERTURB = 1e-5
 OUT = os.path.join(HERE, "precision_fp64_128x48x40.json")
+STEADY_TAU0, STEADY_STEPS = 0.6, 8000
+OUT_STEADY = os.path.join(HERE, "precision_fp64_steady_128x48x40.json")
 
 
-def case():
+def case(tau0=None):
     from windtunnel import f1_config
-    return f1_config(dims=DIMS, h=H, seed=SEED)
+    from windtunnel.engine import make_sim
+    dims, origin, h, sim, shape = f1_config(dims=DIMS, h=H, seed=SEED)
+    if tau0 is not None:
+        sim = make_sim(u_in=sim.u_in, tau0=tau0, smag=sim.smag, sponge_cells=sim.sponge_cells)
+    return dims, origin, h, sim, shape
 
 
 def perturbation(member, n):
@@ -46,9 +59,27 @@ def perturbation(member, n):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--members", type=int, default=4)
+    ap.add_argument("--steady", action="store_true")
     args = ap.parse_args()
     from oracle import pyoracle
     from windtunnel import half_area_cells
+    if args.steady:
+        dims, origin, h, sim, shape = case(STEADY_TAU0)
+        o = pyoracle.Oracle(dims, origin, h, sim, fp64=True)
+        o.voxelize(shape)
+        o.reset()
+        d = o.read(reset_forces=True)
+        blocks = []
+        for k in range(STEADY_STEPS // BLOCK):
+            o.steps(BLOCK)
+            blocks.append((o.read(reset_forces=True)["forces64"] / BLOCK).tolist())
+        rec = {"dims": list(dims), "h": H, "seed": SEED, "tau0": STEADY_TAU0, "steps": STEADY_STEPS, "block": BLOCK,
+               "u_in": sim.u_in, "area_cells": half_area_cells(d["solid"], dims), "guarded": o.guarded(),
+               "reference": "fp64 oracle (oracle/wt_oracle.hpp)", "blocks": blocks}
+        with open(OUT_STEADY, "w") as f:
+            json.dump(rec, f)
+        print("wrote", OUT_STEADY)
+        return
     dims, origin, h, sim, shape = case()
     n = int(np.prod(dims))
     members = []
