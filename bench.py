@@ -10,8 +10,10 @@ One bench step = one frame of the reference engine's compute pass
 per-component forces recorded every step.  Default workload: the generic
 analytic F1 voxelized at 4.5 cm into a 256x96x80 half tunnel (FP32, moving
 belt, heat from brakes/exhaust/radiator at T=1), synthetic geometry from a
-seeded shape.  The lattice (157 MB of populations and cell words) is larger
-than the 126 MB L2, so no flush is needed between timed steps.
+seeded shape.  The FP32 lattice (157 MB of populations and cell words) is
+larger than the 126 MB L2, so no flush is needed between timed steps; a
+working set that fits the L2 (f16 / bf16 at this size: 83 MB) gets an L2
+flush before each timed frame and kernel batch.
 
 value   = MLUPS over the timed frames (inputs resident in HBM, CUDA events on
           the library's stream, max over ranks).
@@ -556,18 +558,50 @@ def main():
     eng.read_forces_raw()
     barrier()
 
+    # Working set against L2.  When the populations and cell words fit the L2
+    # (f16 / bf16 at 256x96x80: 83 MB), every timed frame and every kernel-only
+    # batch starts after a write of twice the L2 size, outside its events; the
+    # steps inside one frame still find the previous step's output in L2, as
+    # they do in any run of that size.
+    l2_bytes = int(getattr(torch.cuda.get_device_properties(local), "L2_cache_size", 126 << 20))
+    ws_bytes = n * (19 * (4 if args.storage == "f32" else 2) + 4)
+    flush_buf = None
+    if ws_bytes < l2_bytes:
+        flush_buf = torch.empty(2 * l2_bytes // 4, dtype=torch.int32, device=torch.device("cuda", local))
+    l2_note = (f"working set (populations + cell words, {ws_bytes / 1e6:.0f} MB) larger than the "
+               f"{l2_bytes / 2**20:.0f} MB L2; no flush" if flush_buf is None else
+               f"working set ({ws_bytes / 1e6:.0f} MB) fits the {l2_bytes / 2**20:.0f} MB L2: a "
+               f"{2 * l2_bytes / 2**20:.0f} MB write flushes it before each timed frame and kernel batch, "
+               f"each timed on its own")
+
+    def timed(fn, count):
+        """Device milliseconds of `count` calls of fn on the engine's stream."""
+        if flush_buf is None:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(count):
+                fn()
+            b.record(stream)
+            barrier()
+            return a.elapsed_time(b)
+        pairs = []
+        for _ in range(count):
+            with torch.cuda.stream(stream):
+                flush_buf.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            pairs.append((a, b))
+        barrier()
+        return sum(a.elapsed_time(b) for a, b in pairs)
+
     # ---- timed device region: K frames, inputs resident in HBM.  The clock
     # sampler stays on through the kernel-only region below, which runs for at
     # least --kernel-seconds of device time, so the clock record holds several
     # samples under load even when K frames take only milliseconds.
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clk = ClockSampler(local).__enter__()
-    e0.record(stream)
-    for _ in range(args.steps):
-        eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0)
-    e1.record(stream)
-    barrier()
-    ms = e0.elapsed_time(e1)
+    ms = timed(lambda: eng.step(lbm_per_frame, 2, lbm_per_frame / 2.0), args.steps)
     ms = max_over_ranks(ms)
     frames = args.steps
     total_cells = n * world
@@ -599,14 +633,8 @@ def main():
     barrier()
     est = p0.elapsed_time(p1) / 4 / 1e3  # seconds per batch
     reps = max(8, int(args.kernel_seconds / max(est, 1e-6)) + 1)
-    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    k0.record(stream)
-    for _ in range(reps):
-        eng.step(ks, 0)
-    k1.record(stream)
-    barrier()
+    kernel_region_ms = timed(lambda: eng.step(ks, 0), reps)
     clk.__exit__(None, None, None)
-    kernel_region_ms = k0.elapsed_time(k1)
     kms = kernel_region_ms / (reps * ks)  # per LBM step (one reduction launch per ks steps included)
     bpl = bytes_per_lup(args.storage)
     achieved = n * bpl / (kms / 1e3) / 1e9
@@ -648,7 +676,7 @@ def main():
             "config": {
                 "workload": desc, "cells": n, "lattice": list(dims), "lbm_steps_per_step": lbm_per_frame,
                 "heat_passes_per_step": 2, "storage": args.storage, "parallelism": f"replicas x{world}",
-                "l2": "working set (populations + cell words) larger than the 126 MB L2; no flush",
+                "l2": l2_note,
                 "block": None if tuned is None else f"{tuned[0]}x{tuned[1]} (autotuned)",
                 "launch": "CUDA graph per frame",
             },
