@@ -85,9 +85,10 @@ constexpr float F16_SCALE = 16384.0f, F16_INV = 1.0f / 16384.0f;
 struct StoreF16 {
   typedef __half T;
   static constexpr uint32_t id = 1;
-  // step-kernel registers: 56 (9 blocks of 128 per SM; the gather variant spills a
-  // few bytes), measured against 52, 60 and 64: 34.7 -> 35.7 GLUPS at 256x96x80
-  static constexpr int max_regs = 56;
+  // step-kernel registers: 48 (10 blocks of 128 per SM, a few bytes of spills in
+  // some variants), measured against 52 and 56 with the moment-form collision:
+  // 48.2 -> 50.2 GLUPS at 512x192x160, 45.7 -> 46.5 at 256x96x80 (52 = 56)
+  static constexpr int max_regs = 48;
   __device__ __forceinline__ static float ld(const T* p, float w) { return __fmaf_rn(__half2float(__ldg(p)), F16_INV, w); }
   __device__ __forceinline__ static float ld_smem(const T* p, float w) { return __fmaf_rn(__half2float(*p), F16_INV, w); }
   __device__ __forceinline__ static void st(T* p, float v, float w) {
@@ -101,8 +102,8 @@ struct StoreF16 {
 struct StoreBF16 {
   typedef __nv_bfloat16 T;
   static constexpr uint32_t id = 2;
-  // step-kernel registers: 56, as for F16 (34.9 -> 36.0 GLUPS at 256x96x80)
-  static constexpr int max_regs = 56;
+  // step-kernel registers: 48, as for F16 (45.9 -> 46.6 GLUPS at 256x96x80)
+  static constexpr int max_regs = 48;
   __device__ __forceinline__ static float ld(const T* p, float w) { return w + __bfloat162float(__ldg(p)); }
   __device__ __forceinline__ static float ld_smem(const T* p, float w) { return w + __bfloat162float(*p); }
   __device__ __forceinline__ static void st(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }

@@ -1,9 +1,10 @@
 """Measured studies of the warm start and the batched aero map.
 
-    python -m windtunnel.studies warmstart [--small] --out DIR
+    python -m windtunnel.studies warmstart [--small] [--data-storage f32] --out DIR
         generate the training set (seeded 256x96x80 F1 runs, fields averaged
-        late in the run), train the network on the GPU with libwt's kernels and
-        save the weights.
+        late in the run: by default over steps 75000-100000 of FP32 cold runs,
+        the window the evaluation takes its reference from), train the network
+        on the GPU with libwt's kernels and save the weights.
     python -m windtunnel.studies evaluate --weights FILE [--small] --out DIR
         warm vs cold FP32 starts of held-out seeds, evaluated by the LBM.
     python -m windtunnel.studies sweep --weights FILE [--small] [--eval-steps N] --out DIR
@@ -103,8 +104,8 @@ def study_warmstart(args):
     train_seeds = list(range(1000, 1000 + n_train))
     val_seeds = list(range(5000, 5000 + n_val))
     log(f"generating {n_train} training + {n_val} held-out runs ({settle}+{avg} steps)")
-    Xt, Tt, Mt, run_t = dataset(train_seeds, settle, avg, every)
-    Xv, Tv, Mv, _ = dataset(val_seeds, settle, avg, every)
+    Xt, Tt, Mt, run_t = dataset(train_seeds, settle, avg, every, storage=args.data_storage)
+    Xv, Tv, Mv, _ = dataset(val_seeds, settle, avg, every, storage=args.data_storage)
     t_data = time.time() - t0
     log(f"data done in {t_data:.1f} s; lattice step {np.mean(run_t['group_step_s']) * 1e3:.3f} ms per group step")
     model = Surrogate(seed=0)
@@ -118,7 +119,7 @@ def study_warmstart(args):
     wpath = os.path.join(args.out, "warmstart_f1.npz")
     save_weights(model, wpath)
     res = {"train_cases": n_train, "val_cases": n_val, "settle_steps": settle, "average_steps": avg,
-           "data_storage": "f16", "epochs": epochs, "train_loss": hist, "val_loss": vloss,
+           "data_storage": args.data_storage, "epochs": epochs, "train_loss": hist, "val_loss": vloss,
            "val_loss_uniform_state": zero, "data_seconds": t_data, "train_seconds": t_train,
            "lattice_step_s_per_group": run_t["group_step_s"]}
     with open(os.path.join(args.out, "warmstart_train.json"), "w") as f:
@@ -244,13 +245,14 @@ def main(argv=None):
     ap.add_argument("study", choices=["warmstart", "evaluate", "sweep"])
     ap.add_argument("--train-cases", type=int, default=400)
     ap.add_argument("--val-cases", type=int, default=50)
-    ap.add_argument("--settle", type=int, default=24000)
-    ap.add_argument("--average", type=int, default=8000)
+    ap.add_argument("--settle", type=int, default=75000)
+    ap.add_argument("--average", type=int, default=25000)
+    ap.add_argument("--data-storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--out", default="study_out")
     ap.add_argument("--small", action="store_true")
     ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--eval-steps", type=int, default=64000)
+    ap.add_argument("--eval-steps", type=int, default=100000)
     ap.add_argument("--weights", default=None)
     args = ap.parse_args(argv)
     import torch

@@ -1,12 +1,25 @@
-"""What the trained warm start gains over the cold start, evaluated by the LBM.
+"""What the trained warm start gains over the cold start, judged by the LBM.
 
-The committed network (windtunnel/data/warmstart_f1.npz, trained on seeds
-1000-1399) predicts the coarse flow of two held-out cars (seeds 5000 and 5003);
-the prediction replaces the uniform initial state through wt_reset_from.  A
-long cold FP32 run of each car gives the late-time reference (mean over steps
-18000-24000).  Over steps 2000-8000 the warm run's mean Cd and Cl must be
-closer to that reference than the cold run's, and its predicted coarse field
-closer to the cold run's late coarse field than the uniform inlet state is."""
+The committed network (windtunnel/data/warmstart_f1.npz) was trained on 100
+seeded cars (seeds 1000-1099), its targets the coarse (u, rho) fields of their
+cold FP32 runs averaged over steps 75000-100000: the same window the judge's
+reference comes from.  For two held-out cars (seeds 5003 and 5029) a cold and a
+warm-started FP32 run go 100000 steps; the reference is the mean of the cold
+run's Cd and Cl over its last quarter, and a run has converged at the first
+step after which its trailing 5760-step means of Cd and Cl stay within 1 % of
+it (windtunnel/warmstart.py).
+
+Asserted, as recorded over the 50 held-out seeds in
+profiles/warmstart_eval_f1.json:
+  * the prediction is much closer to the cold run's late coarse field than the
+    uniform inlet state is;
+  * the cold runs converge at the recorded steps (55488 and 34247);
+  * the warm-started runs do not converge: they settle in another long-lived
+    flow state, more than 1 % from the cold reference in Cd or Cl at the end.
+So the steps saved to 1 % are not positive: the LBM judge rejects this warm
+start and the cold start (LBM_INIT, src/engine/wgsl.ts:141-155) remains the
+path that gives the reference's answer."""
+import json
 import os
 
 import numpy as np
@@ -16,7 +29,9 @@ pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
-SEEDS = (5000, 5003)
+SEEDS = (5003, 5029)
+HORIZON = 100000
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.fixture(scope="module")
@@ -28,15 +43,17 @@ def runs(wt_lib):
     shapes = [ws.case_shape(s) for s in SEEDS]
     cases = [(ws.F1_DIMS, ws.F1_H, sh) for sh in shapes]
     fields = warm_fields(model, shapes)
-    cold = ws.run_cases(cases, 24000, storage="f32", average=(16000, 2000))
-    warm = ws.run_cases(cases, 8000, warm=fields, storage="f32")
-    return ws, fields, cold, warm
+    cold = ws.run_cases(cases, HORIZON, storage="f32", average=(75000, 500))
+    warm = ws.run_cases(cases, HORIZON, warm=fields, storage="f32")
+    with open(os.path.join(ROOT, "profiles", "warmstart_eval_f1.json")) as f:
+        record = {r["seed"]: r for r in json.load(f)["cases"]}
+    return ws, fields, cold, warm, record
 
 
 def test_prediction_is_closer_than_uniform_state(runs):
-    ws, fields, cold, _ = runs
+    ws, fields, cold, _, _ = runs
     for k in range(len(SEEDS)):
-        late = cold["coarse"][k]            # [20, 24, 64, 4], mean over steps 16000-24000
+        late = cold["coarse"][k]            # [20, 24, 64, 4], mean over steps 75000-100000
         fluid = late[..., 3] != 1.0
         uniform = np.zeros_like(late)
         uniform[..., 0], uniform[..., 3] = ws.U_IN, 1.0
@@ -46,14 +63,19 @@ def test_prediction_is_closer_than_uniform_state(runs):
         assert e_pred < 0.5 * e_unif
 
 
-def test_warm_start_forces_closer_to_late_values(runs):
-    ws, _, cold, warm = runs
-    for k in range(len(SEEDS)):
-        ref_cd, ref_cl = float(np.mean(cold["cd"][k][18000:])), float(np.mean(cold["cl"][k][18000:]))
-        c_cd, c_cl = float(np.mean(cold["cd"][k][2000:8000])), float(np.mean(cold["cl"][k][2000:8000]))
-        w_cd, w_cl = float(np.mean(warm["cd"][k][2000:8000])), float(np.mean(warm["cl"][k][2000:8000]))
-        err_c = abs(c_cd - ref_cd) / abs(ref_cd) + abs(c_cl - ref_cl) / abs(ref_cl)
-        err_w = abs(w_cd - ref_cd) / abs(ref_cd) + abs(w_cl - ref_cl) / abs(ref_cl)
-        print(f"\nseed {SEEDS[k]}: late Cd {ref_cd:.3f} Cl {ref_cl:.3f}; steps 2000-8000 cold Cd {c_cd:.3f} "
-              f"Cl {c_cl:.3f} (error {err_c:.3f}), warm Cd {w_cd:.3f} Cl {w_cl:.3f} (error {err_w:.3f})")
-        assert err_w < err_c
+def test_warm_start_steps_to_one_percent(runs):
+    ws, _, cold, warm, record = runs
+    for k, seed in enumerate(SEEDS):
+        ref_cd, ref_cl = ws.reference_values(cold["cd"][k], cold["cl"][k])
+        c = ws.convergence_step(cold["cd"][k], cold["cl"][k], ref_cd, ref_cl)
+        w = ws.convergence_step(warm["cd"][k], warm["cl"][k], ref_cd, ref_cl)
+        end_cd = float(ws.trailing_mean(warm["cd"][k])[-1])
+        end_cl = float(ws.trailing_mean(warm["cl"][k])[-1])
+        print(f"\nseed {seed}: reference Cd {ref_cd:.4f} Cl {ref_cl:.4f}; cold converges at {c}, warm at {w} "
+              f"(warm ends at Cd {end_cd:.4f} Cl {end_cl:.4f})")
+        rec = record[seed]
+        assert abs(ref_cd - rec["ref_cd"]) <= 1e-9 * abs(rec["ref_cd"])
+        assert abs(ref_cl - rec["ref_cl"]) <= 1e-9 * abs(rec["ref_cl"])
+        assert c is not None and abs(c - rec["cold_steps"]) <= 64
+        assert w is None and rec["warm_steps"] is None
+        assert abs(end_cd - ref_cd) > 0.01 * abs(ref_cd) or abs(end_cl - ref_cl) > 0.01 * abs(ref_cl)
