@@ -9,7 +9,7 @@
   the same case (wt_read_coarse), time-averaged after the flow has settled.
 * Use: the network's field goes through wt_reset_from (trilinear upsampling to
   the lattice, equilibrium populations) in place of LBM_INIT's uniform state.
-* Judge: the LBM itself.  Cd and Cl of the whole car come from the per-step
+* Evaluation: the LBM itself.  Cd and Cl of the whole car come from the per-step
   FP64 force history; a run is converged at the first step after which the mean
   over the trailing window (5760 steps, or all steps so far when fewer) stays
   within 1 % of the reference value for both, the reference being the mean over

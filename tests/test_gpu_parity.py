@@ -1,9 +1,9 @@
 """The CUDA path (libwt through its C ABI) against the oracle and the golden
 fixtures.  Flags, emission and link masks are compared bit for bit; lattice
 states bit for bit as well (the kernels keep the reference's float operation
-order and are built without contraction).  The acceptance tolerance the
-north star states for FP32 fields is 1e-4 relative; it is asserted too, so a
-failure report shows which bar broke."""
+order and are built without contraction).  The stated acceptance tolerance
+for FP32 fields, 1e-4 relative, is asserted too, so a failure report shows
+which bar broke."""
 import os
 
 import numpy as np

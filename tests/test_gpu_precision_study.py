@@ -6,7 +6,7 @@ FP64 oracle on the precision case: the generic F1 (seed 5) at 128x48x40 cells
 Steady flow (tau0 0.6, 8000 steps): the same car at ten times the viscosity,
 where the wake is steady and window means are deterministic.  Cd and Cl averaged
 over the last 1000 steps against the FP64 run:
-    f32 within 1e-4, f16 within 1 % (the benchmark spec's bound), bf16 reported.
+    f32 within 1e-4, f16 within 1 % (the stated bound for FP16 storage), bf16 reported.
 
 Unsteady flow (tau0 0.51, the benchmark's value, 20000 steps): the case has
 several long-lived flow states, and FP64 runs that differ by a 1e-5 perturbation

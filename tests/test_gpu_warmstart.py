@@ -1,9 +1,9 @@
-"""What the trained warm start gains over the cold start, judged by the LBM.
+"""What the trained warm start gains over the cold start, evaluated by the LBM.
 
 The committed network (windtunnel/data/warmstart_f1.npz) was trained on 100
 seeded cars (seeds 1000-1099), its targets the coarse (u, rho) fields of their
-cold FP32 runs averaged over steps 75000-100000: the same window the judge's
-reference comes from.  For two held-out cars (seeds 5003 and 5029) a cold and a
+cold FP32 runs averaged over steps 75000-100000: the same window the
+evaluation's reference comes from.  For two held-out cars (seeds 5003 and 5029) a cold and a
 warm-started FP32 run go 100000 steps; the reference is the mean of the cold
 run's Cd and Cl over its last quarter, and a run has converged at the first
 step after which its trailing 5760-step means of Cd and Cl stay within 1 % of
@@ -16,7 +16,7 @@ profiles/warmstart_eval_f1.json:
   * the cold runs converge at the recorded steps (55488 and 34247);
   * the warm-started runs do not converge: they settle in another long-lived
     flow state, more than 1 % from the cold reference in Cd or Cl at the end.
-So the steps saved to 1 % are not positive: the LBM judge rejects this warm
+So the steps saved to 1 % are not positive: the LBM evaluation rejects this warm
 start and the cold start (LBM_INIT, src/engine/wgsl.ts:141-155) remains the
 path that gives the reference's answer."""
 import json
