@@ -399,15 +399,18 @@ struct OfsCalc {
 };
 
 // L2 prefetch of the tile a.prefetch_ahead blocks further on (about one wave of
-// resident blocks ahead, in launch order): thread t < 19 * by issues one bulk
-// prefetch of direction t % 19 over row t / 19 of that tile, so DRAM streams the
-// next wave's own-cell rows while this wave computes.  The byte range is
-// widened to 16-byte boundaries and clipped to the population allocation.
-template <class T>
+// resident blocks ahead, in launch order; REV: tiles run in reverse order): thread
+// t < 19 * by issues one bulk prefetch of direction t % 19 over row t / 19 of
+// that tile, so DRAM streams the next wave's own-cell rows while this wave
+// computes.  The byte range is widened to 16-byte boundaries and clipped to the
+// population allocation.
+template <class T, bool REV>
 __device__ __forceinline__ void prefetch_tile(const StepArgs& a, uint3 bid, uint3 gdim) {
   if (a.prefetch_ahead == 0) return;
   const uint32_t nb = gdim.x * gdim.y * gdim.z;
-  const uint32_t tb = bid.x + gdim.x * (bid.y + gdim.y * bid.z) + a.prefetch_ahead;
+  const uint32_t lin = bid.x + gdim.x * (bid.y + gdim.y * bid.z);
+  if (REV && lin < a.prefetch_ahead) return;
+  const uint32_t tb = REV ? lin - a.prefetch_ahead : lin + a.prefetch_ahead;
   const uint32_t t = threadIdx.x + blockDim.x * threadIdx.y;
   if (tb >= nb || t >= 19u * blockDim.y) return;
   const uint32_t dir = t % 19u, row = t / 19u;
@@ -427,7 +430,7 @@ __device__ __forceinline__ void prefetch_tile(const StepArgs& a, uint3 bid, uint
 
 // One block's cells of one lattice.  bid/gdim are the block coordinates and grid
 // of that lattice's tiling; slots is where this step's force records go.
-template <class St, bool GATHER, bool FIELDS, class Ofs>
+template <class St, bool GATHER, bool FIELDS, class Ofs, bool REV = false>
 __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, ForceSlot* slots, uint3 bid, uint3 gdim) {
   const uint8_t* __restrict__ solid_u8 = a.solid;
   const uint32_t nx = a.nx, ny = a.ny, nz = a.nz;
@@ -437,7 +440,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
   const bool in = (x < nx) && (y < ny);
   const uint32_t nxy = nx * ny;
   const uint32_t np = (uint32_t)a.np;
-  if constexpr (Ofs::plain_path) prefetch_tile<typename St::T>(a, bid, gdim);
+  if constexpr (Ofs::plain_path) prefetch_tile<typename St::T, REV>(a, bid, gdim);
   const uint32_t idx = in ? x + nx * y + nxy * z : 0u;
   const uint32_t cw = in ? __ldg(a.cellw + idx) : CW_SOLID;
   typedef typename St::T PT;
@@ -721,7 +724,18 @@ cudaError_t launch_chained(K kernel, dim3 grid, dim3 block, cudaStream_t s, Args
 template <class St, bool GATHER, bool FIELDS>
 __global__ void __maxnreg__(St::max_regs) step_kernel(StepArgs a) {
   chain_enter();
-  step_tile<St, GATHER, FIELDS>(a, OfsTable{a}, a.slots, blockIdx, make_uint3(gridDim.x, gridDim.y, gridDim.z));
+  // Local steps take the tiles in reverse launch order: their first tiles are the
+  // ones the preceding gather step ran last, whose lines are still in the L2
+  // (the FP32 lattice at 256x96x80, 157 MB of populations, is larger than the
+  // L2).  Force and mass records are keyed by tile coordinates, not by launch
+  // order, so the results do not change.
+  const uint3 gdim = make_uint3(gridDim.x, gridDim.y, gridDim.z);
+  if constexpr (GATHER) {
+    step_tile<St, GATHER, FIELDS, OfsTable, false>(a, OfsTable{a}, a.slots, blockIdx, gdim);
+  } else {
+    const uint3 bid = make_uint3(gdim.x - 1 - blockIdx.x, gdim.y - 1 - blockIdx.y, gdim.z - 1 - blockIdx.z);
+    step_tile<St, GATHER, FIELDS, OfsTable, true>(a, OfsTable{a}, a.slots, bid, gdim);
+  }
 }
 
 // Many lattices in one launch: block b belongs to the lattice L with
