@@ -5,6 +5,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -145,7 +146,7 @@ int bfail(wt_batch* b, int code, const std::string& m) {
   } while (0)
 
 uint64_t batch_version(const wt_batch* b) {
-  uint64_t v = ((uint64_t)b->bx << 32) ^ ((uint64_t)b->by << 48);
+  uint64_t v = ((uint64_t)b->bx << 32) ^ ((uint64_t)b->by << 48) ^ ((uint64_t)b->persist << 62);
   for (auto* c : b->lat) v = v * 1000003ull + c->version + ((uint64_t)c->bx << 40) + ((uint64_t)c->by << 52);
   return v;
 }
@@ -182,6 +183,7 @@ int refresh_batch(wt_batch* b) {
   }
   b->total_blocks = base;
   b->pending_cap = cap;
+  b->persist_grid = std::min(base, batch_persist_blocks(b->storage, dim3(b->bx, b->by, 1), b->lat[0]->sm_count));
   WT_BCUDA(b, cudaMemcpyAsync(b->d_args, args.data(), count * sizeof(StepArgs), cudaMemcpyHostToDevice, b->stream));
   WT_BCUDA(b, cudaMemcpyAsync(b->d_tiles, tiles.data(), count * sizeof(BatchTiles), cudaMemcpyHostToDevice, b->stream));
   WT_BCUDA(b, cudaMemcpyAsync(b->d_reduce, red.data(), count * sizeof(ReduceArgs), cudaMemcpyHostToDevice, b->stream));
@@ -196,16 +198,39 @@ cudaError_t enqueue_batch(wt_batch* b, int n, int heat_passes, float dt, cudaStr
   for (auto* c : b->lat)  // the tables were built for exactly this shape
     if (c->geom.block.x != block.x || c->geom.block.y != block.y) return cudaErrorInvalidConfiguration;
   uint32_t pending = 0;
-  for (int k = 0; k < n; k++) {
-    const bool last = (k == n - 1);
-    cudaError_t e = launch_batch_step(b->storage, (k & 1) == 0, last, block, b->total_blocks, b->d_args, b->d_tiles,
-                                      count, pending, s);
-    if (e != cudaSuccess) return e;
-    pending++;
-    if (pending == b->pending_cap || last) {
-      e = launch_force_reduce(b->d_reduce, count, pending, last, s);
+  if (b->persist && b->persist_grid) {
+    // one cooperative launch per run of steps that fills the force records
+    for (uint32_t k = 0; k < (uint32_t)n;) {
+      const uint32_t chunk = std::min((uint32_t)n - k, b->pending_cap - pending);
+      const bool last = k + chunk == (uint32_t)n;
+      cudaError_t e = cudaMemsetAsync(b->d_sync, 0, sizeof(unsigned int), s);
+      if (e == cudaSuccess)
+        e = launch_batch_persist(b->storage, block, b->persist_grid, b->total_blocks, b->d_args, b->d_tiles, count, k,
+                                 chunk, pending, last, b->d_sync, s);
       if (e != cudaSuccess) return e;
-      pending = 0;
+      pending += chunk;
+      k += chunk;
+      if (pending == b->pending_cap || last) {
+        e = launch_force_reduce(b->d_reduce, count, pending, last, s);
+        if (e != cudaSuccess) return e;
+        pending = 0;
+      }
+    }
+    // the barrier's expiry flag, read back by the next call
+    cudaError_t e = cudaMemcpyAsync(b->h_flag, b->d_sync + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+  } else {
+    for (int k = 0; k < n; k++) {
+      const bool last = (k == n - 1);
+      cudaError_t e = launch_batch_step(b->storage, (k & 1) == 0, last, block, b->total_blocks, b->d_args,
+                                        b->d_tiles, count, pending, s);
+      if (e != cudaSuccess) return e;
+      pending++;
+      if (pending == b->pending_cap || last) {
+        e = launch_force_reduce(b->d_reduce, count, pending, last, s);
+        if (e != cudaSuccess) return e;
+        pending = 0;
+      }
     }
   }
   for (auto* c : b->lat) {
@@ -236,10 +261,18 @@ int wt_batch_create(const wt_grid* grids, uint32_t count, const wt_sim* sim, wt_
   }
   if (cudaMalloc((void**)&b->d_args, count * sizeof(StepArgs)) != cudaSuccess ||
       cudaMalloc((void**)&b->d_tiles, count * sizeof(BatchTiles)) != cudaSuccess ||
-      cudaMalloc((void**)&b->d_reduce, count * sizeof(ReduceArgs)) != cudaSuccess) {
+      cudaMalloc((void**)&b->d_reduce, count * sizeof(ReduceArgs)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_sync, 2 * sizeof(unsigned int)) != cudaSuccess ||
+      cudaHostAlloc((void**)&b->h_flag, sizeof(unsigned int), cudaHostAllocDefault) != cudaSuccess) {
     b->err = "wt_batch_create: device tables";
     return cleanup(WT_ERR_NOMEM);
   }
+  *b->h_flag = 0u;
+  if (cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned int), b->stream) != cudaSuccess) {
+    b->err = "wt_batch_create: cudaMemsetAsync";
+    return cleanup(WT_ERR_CUDA);
+  }
+  if (const char* e = getenv("WT_BATCH_PERSIST")) b->persist = atoi(e) != 0;
   int rc = refresh_batch(b);
   if (rc) return cleanup(rc);
   *out = b;
@@ -255,6 +288,8 @@ int wt_batch_destroy(wt_batch* b) {
   if (b->d_args) cudaFree(b->d_args);
   if (b->d_tiles) cudaFree(b->d_tiles);
   if (b->d_reduce) cudaFree(b->d_reduce);
+  if (b->d_sync) cudaFree(b->d_sync);
+  if (b->h_flag) cudaFreeHost(b->h_flag);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return WT_OK;
@@ -269,6 +304,10 @@ int wt_batch_step(wt_batch* b, int n_lbm_steps, int heat_passes, float heat_dt) 
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, WT_ERR_CUDA, "cudaSetDevice");
   if (n_lbm_steps < 2 || (n_lbm_steps & 1)) return bfail(b, WT_ERR_ARG, "wt_batch_step: n_lbm_steps must be even and >= 2");
   if (heat_passes < 0 || (heat_passes & 1)) return bfail(b, WT_ERR_ARG, "wt_batch_step: heat_passes must be 0 or even");
+  if (*b->h_flag) {  // written by an earlier call's persistent launch (see enqueue_batch)
+    *b->h_flag = 0u;
+    return bfail(b, WT_ERR_CUDA, "wt_batch_step: a grid barrier of the persistent launch timed out");
+  }
   int rc = refresh_batch(b);
   if (rc) return rc;
   const float dt = heat_dt > 0.0f ? heat_dt : (float)n_lbm_steps / 2.0f;
@@ -297,18 +336,27 @@ int wt_batch_tune(wt_batch* b, uint32_t* bx_out, uint32_t* by_out, float* ms_out
   }
   float best = 1e30f;
   uint32_t bbx = b->bx, bby = b->by;
+  bool bpersist = b->persist;
+  // launch per step, and the persistent launch, unless WT_BATCH_PERSIST fixes it
+  std::vector<bool> modes{b->persist};
+  if (!getenv("WT_BATCH_PERSIST")) modes = {false, true};
   for (auto& sh : kShapes) {
-    b->bx = sh[0];
-    b->by = sh[1];
-    const float ms = time_steps(b->stream, [&](int n) { return wt_batch_step(b, n, 0, 0.0f); });
-    if (ms > 0.0f && ms < best) {
-      best = ms;
-      bbx = b->bx;
-      bby = b->by;
+    for (bool persist : modes) {
+      b->bx = sh[0];
+      b->by = sh[1];
+      b->persist = persist;
+      const float ms = time_steps(b->stream, [&](int n) { return wt_batch_step(b, n, 0, 0.0f); });
+      if (ms > 0.0f && ms < best) {
+        best = ms;
+        bbx = b->bx;
+        bby = b->by;
+        bpersist = persist;
+      }
     }
   }
   b->bx = bbx;
   b->by = bby;
+  b->persist = bpersist;
   int rc = refresh_batch(b);
   if (rc) return rc;
   for (size_t i = 0; i < b->lat.size(); i++) {
@@ -323,6 +371,8 @@ int wt_batch_tune(wt_batch* b, uint32_t* bx_out, uint32_t* by_out, float* ms_out
 }
 
 void* wt_batch_stream(wt_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+uint32_t wt_batch_persistent_grid(const wt_batch* b) { return (b && b->persist) ? b->persist_grid : 0u; }
 
 const char* wt_batch_last_error(const wt_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
 

@@ -105,6 +105,12 @@ struct wt_batch {
   wt::ReduceArgs* d_reduce = nullptr;
   uint32_t total_blocks = 0;
   uint32_t pending_cap = 1;
+  // persistent launch (batch_persist_kernel): on/off, its grid, the grid
+  // barrier's device words and the pinned copy of the barrier's expiry flag
+  bool persist = false;
+  uint32_t persist_grid = 0;
+  unsigned int* d_sync = nullptr;
+  unsigned int* h_flag = nullptr;
   uint64_t version = ~0ull;                // sum of member versions the device tables were built for
   std::vector<wt_ctx::Graph> graphs;
   std::string err;

@@ -104,6 +104,16 @@ cudaError_t launch_step(uint32_t storage, bool gather, bool write_fields, const 
 cudaError_t launch_batch_step(uint32_t storage, bool gather, bool write_fields, dim3 block, uint32_t total_blocks,
                               const StepArgs* args, const BatchTiles* tiles, uint32_t count, uint32_t pending,
                               cudaStream_t s);
+// Persistent batch: one cooperative launch advances every lattice by nsteps
+// (<= WT_PENDING_MAX) steps, step k0 + k of the call being a gather step when
+// even; sync[0] is the grid barrier's counter (zero before the launch), sync[1]
+// is raised if a barrier wait expires.  grid = batch_persist_blocks(...), the
+// blocks that can be resident at once (0: not available).
+uint32_t batch_persist_blocks(uint32_t storage, dim3 block, uint32_t sm_count);
+cudaError_t launch_batch_persist(uint32_t storage, dim3 block, uint32_t grid, uint32_t total_blocks,
+                                 const StepArgs* args, const BatchTiles* tiles, uint32_t count, uint32_t k0,
+                                 uint32_t nsteps, uint32_t pending0, bool fields_last, unsigned int* sync,
+                                 cudaStream_t s);
 // Per-lattice arguments of the force reduction (one record per lattice, in device memory).
 struct ReduceArgs {
   const ForceSlot* slots;

@@ -72,6 +72,9 @@ struct StoreF32 {
   // against 48 (5 blocks of 256, small spills) to 64: 71.2 % -> 73.6 % of HBM
   static constexpr int max_regs = 56;
   __device__ __forceinline__ static float ld(const T* p, float) { return __ldg(p); }
+  // L2-coherent load (ld.global.cg): for populations another block may have
+  // rewritten earlier in the same launch (the persistent batch kernel)
+  __device__ __forceinline__ static float ld_coh(const T* p, float) { return __ldcg(p); }
   __device__ __forceinline__ static float ld_smem(const T* p, float) { return *p; }
   __device__ __forceinline__ static void st(T* p, float v, float) { *p = v; }
 };
@@ -97,6 +100,7 @@ struct StoreF16 {
   // the stored deviation itself, in units of 2^-14 (the step kernel's working form)
   static constexpr float S = F16_SCALE;
   __device__ __forceinline__ static float ldd(const T* p) { return __half2float(__ldg(p)); }
+  __device__ __forceinline__ static float ldd_coh(const T* p) { return __half2float(__ldcg(p)); }
   __device__ __forceinline__ static void std_(T* p, float d) { *p = __float2half_rn(d); }
 };
 struct StoreBF16 {
@@ -109,6 +113,7 @@ struct StoreBF16 {
   __device__ __forceinline__ static void st(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
   static constexpr float S = 1.0f;
   __device__ __forceinline__ static float ldd(const T* p) { return __bfloat162float(__ldg(p)); }
+  __device__ __forceinline__ static float ldd_coh(const T* p) { return __bfloat162float(__ldcg(p)); }
   __device__ __forceinline__ static void std_(T* p, float d) { *p = __float2bfloat16_rn(d); }
 };
 

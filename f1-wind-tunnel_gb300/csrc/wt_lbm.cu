@@ -300,11 +300,17 @@ __device__ __forceinline__ CellOut collide_dev(const float (&d)[19], float (&fo)
 // storage (with the reference's arithmetic in collide(), bit for bit), scaled
 // deviations d_i = S (f_i - w_i) for f16 / bf16 storage (their stored form,
 // collided by collide_dev).  Boundary values come in the same form.
-template <class St>
+// NC: populations are loaded through the read-only (non-coherent) path, valid
+// when no block rewrites them during the launch; the persistent batch kernel,
+// whose steps rewrite them, loads with NC = false (L2-coherent loads).
+template <class St, bool NC = true>
 struct Rep {
   typedef typename St::T T;
   static constexpr bool dev = false;
-  __device__ __forceinline__ static float ld(const T* p, int dir) { return St::ld(p, Wd(dir)); }
+  __device__ __forceinline__ static float ld(const T* p, int dir) {
+    if constexpr (NC) return St::ld(p, Wd(dir));
+    else return St::ld_coh(p, Wd(dir));
+  }
   __device__ __forceinline__ static void st(T* p, float v, int dir) { St::st(p, v, Wd(dir)); }
   __device__ __forceinline__ static float solid(int k) { return Wd(k); }  // wgsl.ts:183
   __device__ __forceinline__ static float feq_in(const StepArgs& a, int i) { return a.feq_in[i]; }
@@ -314,11 +320,14 @@ struct Rep {
   }
   template <int i> __device__ __forceinline__ static float link_t(float v) { return 2.0f * (v - Wd(i)); }
 };
-template <class St>
+template <class St, bool NC = true>
 struct RepDev {
   typedef typename St::T T;
   static constexpr bool dev = true;
-  __device__ __forceinline__ static float ld(const T* p, int) { return St::ldd(p); }
+  __device__ __forceinline__ static float ld(const T* p, int) {
+    if constexpr (NC) return St::ldd(p);
+    else return St::ldd_coh(p);
+  }
   __device__ __forceinline__ static void st(T* p, float v, int) { St::std_(p, v); }
   __device__ __forceinline__ static float solid(int) { return 0.0f; }
   __device__ __forceinline__ static float feq_in(const StepArgs& a, int i) { return a.dev_in[i]; }
@@ -328,13 +337,13 @@ struct RepDev {
   }
   template <int i> __device__ __forceinline__ static float link_t(float v) { return v * (2.0f / St::S); }
 };
-template <> struct Rep<StoreF16> : RepDev<StoreF16> {};
-template <> struct Rep<StoreBF16> : RepDev<StoreBF16> {};
+template <bool NC> struct Rep<StoreF16, NC> : RepDev<StoreF16, NC> {};
+template <bool NC> struct Rep<StoreBF16, NC> : RepDev<StoreBF16, NC> {};
 
 // A population of direction dir at cell index `cell` in the step's form.
-template <class St>
+template <class St, bool NC = true>
 __device__ __forceinline__ float ldr(const void* pop, int dir, uint32_t np, uint32_t cell) {
-  return Rep<St>::ld(reinterpret_cast<const typename St::T*>(pop) + (size_t)dir * np + cell, dir);
+  return Rep<St, NC>::ld(reinterpret_cast<const typename St::T*>(pop) + (size_t)dir * np + cell, dir);
 }
 template <class St>
 __device__ __forceinline__ void str(void* pop, int dir, uint32_t np, uint32_t cell, float v, int wdir) {
@@ -430,7 +439,9 @@ __device__ __forceinline__ void prefetch_tile(const StepArgs& a, uint3 bid, uint
 
 // One block's cells of one lattice.  bid/gdim are the block coordinates and grid
 // of that lattice's tiling; slots is where this step's force records go.
-template <class St, bool GATHER, bool FIELDS, class Ofs, bool REV = false>
+// LOOP: the block goes on to another tile after this one (persistent batch
+// kernel), so the shared force arrays are released with a barrier at the end.
+template <class St, bool GATHER, bool FIELDS, class Ofs, bool REV = false, bool LOOP = false>
 __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, ForceSlot* slots, uint3 bid, uint3 gdim) {
   const uint8_t* __restrict__ solid_u8 = a.solid;
   const uint32_t nx = a.nx, ny = a.ny, nz = a.nz;
@@ -444,7 +455,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
   const uint32_t idx = in ? x + nx * y + nxy * z : 0u;
   const uint32_t cw = in ? __ldg(a.cellw + idx) : CW_SOLID;
   typedef typename St::T PT;
-  typedef Rep<St> R;
+  typedef Rep<St, !LOOP> R;
   PT* __restrict__ P = reinterpret_cast<PT*>(a.pop);
   float gf[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   float rho_cell = 0.0f;
@@ -487,7 +498,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
       sfor<19>([&](auto I) {
         constexpr int i = I;
         if constexpr (i == 0) {
-          f[0] = ldr<St>(a.pop, 0, np, idx);
+          f[0] = ldr<St, !LOOP>(a.pop, 0, np, idx);
         } else if constexpr (GATHER) {
           constexpr int off_x = CXd(i), off_y = CYd(i), off_z = CZd(i);
           const int off = off_x + off_y * (int)nx + off_z * (int)nxy;
@@ -496,7 +507,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
           const int wdir = bb ? i : OPPd(i);
           f[i] = R::ld(reinterpret_cast<const typename St::T*>(a.pop) + slot, wdir);
         } else {
-          f[i] = ldr<St>(a.pop, i, np, idx);
+          f[i] = ldr<St, !LOOP>(a.pop, i, np, idx);
         }
       });
     } else {
@@ -504,7 +515,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
         constexpr int i = I;
         constexpr int cx = CXd(i), cy = CYd(i), cz = CZd(i);
         if constexpr (i == 0) {
-          f[0] = ldr<St>(a.pop, 0, np, idx);
+          f[0] = ldr<St, !LOOP>(a.pop, 0, np, idx);
         } else {
           float v;
           if (cx > 0 && x == 0) {
@@ -512,21 +523,21 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
           } else if (cx < 0 && x == nx - 1) {
             v = R::template outlet<i>(pu.x, pu.y, pu.z);
           } else if (cy > 0 && y == 0) {
-            v = ldr<St>(a.pop, i, np, idx);
+            v = ldr<St, !LOOP>(a.pop, i, np, idx);
             if constexpr (cx != 0) v = v + R::floor_k(a, i) * floor_u;
           } else if ((cy < 0 && y == ny - 1) || (cz < 0 && z == nz - 1)) {
             v = R::feq_in(a, i);
           } else if (GATHER) {
             if ((cw >> i) & 1u) {
-              v = ldr<St>(a.pop, i, np, idx);
+              v = ldr<St, !LOOP>(a.pop, i, np, idx);
             } else if (cz > 0 && z == 0) {
-              v = ldr<St>(a.pop, OPPd(ZMIRd(i)), np, (uint32_t)((int)idx - cx - cy * (int)nx));
+              v = ldr<St, !LOOP>(a.pop, OPPd(ZMIRd(i)), np, (uint32_t)((int)idx - cx - cy * (int)nx));
             } else {
               const int off = cx + cy * (int)nx + cz * (int)nxy;
-              v = ldr<St>(a.pop, OPPd(i), np, (uint32_t)((int)idx - off));
+              v = ldr<St, !LOOP>(a.pop, OPPd(i), np, (uint32_t)((int)idx - off));
             }
           } else {
-            v = ldr<St>(a.pop, i, np, idx);
+            v = ldr<St, !LOOP>(a.pop, i, np, idx);
           }
           f[i] = v;
         }
@@ -694,6 +705,7 @@ __device__ __forceinline__ void step_tile(const StepArgs& a, const Ofs& ofs, For
       out.raw[q] = (int32_t)tt;
     }
   }
+  if constexpr (LOOP) __syncthreads();  // thread 0 has read s_f / s_r before the next tile writes them
 }
 
 // Consecutive collide-stream launches are chained by programmatic dependent
@@ -759,6 +771,76 @@ __global__ void __maxnreg__(St::max_regs) batch_step_kernel(const StepArgs* __re
   const StepArgs& a = args[lo];
   const OfsCalc ofs{(uint32_t)a.np};
   step_tile<St, GATHER, FIELDS>(a, ofs, a.slots + (size_t)pending * a.nslots, bid, gdim);
+}
+
+// Persistent batch: ONE cooperative launch advances every lattice of the batch
+// by nsteps LBM steps (at most the pending force-record capacity).  Each step
+// walks all tiles of all lattices grid-stride in launch order, with the
+// per-tile arithmetic and records of batch_step_kernel, so the results are the
+// same bits; a grid barrier separates the steps.  The barrier's wait is bounded:
+// on expiry the block raises sync[1] and leaves the kernel (the host reports
+// the flag), so a failure ends the launch instead of hanging it.  The launch is
+// cooperative, so all blocks are resident and every barrier can be met.
+constexpr uint32_t BARRIER_POLLS = 1u << 22;  // x ~100 ns: ~0.4 s against ~2 ms steps
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const unsigned int* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* sync, uint32_t target) {
+  __shared__ uint32_t s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    atomicAdd(sync, 1u);
+    uint32_t ok = 0;
+    for (uint32_t i = 0; i < BARRIER_POLLS; i++) {
+      if (ld_acquire_u32(sync) >= target) {
+        ok = 1;
+        break;
+      }
+      __nanosleep(100);
+    }
+    if (!ok) atomicExch(sync + 1, 1u);
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// (FP32: 8 registers above the step kernel's cap, 112 B of spills instead of 296)
+template <class St>
+__global__ void __maxnreg__(St::max_regs + (St::id == WT_STORE_F32 ? 8 : 0)) batch_persist_kernel(const StepArgs* __restrict__ args,
+                                                               const BatchTiles* __restrict__ tiles, uint32_t count,
+                                                               uint32_t total, uint32_t k0, uint32_t nsteps,
+                                                               uint32_t pending0, uint32_t fields_last,
+                                                               unsigned int* sync) {
+  for (uint32_t k = 0; k < nsteps; k++) {
+    const bool gather = ((k0 + k) & 1u) == 0u;
+    const bool fields = fields_last && k + 1 == nsteps;
+    for (uint32_t b = blockIdx.x; b < total; b += gridDim.x) {
+      uint32_t lo = 0, hi = count;  // largest L with base[L] <= b
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&tiles[mid].base) <= b) lo = mid;
+        else hi = mid;
+      }
+      const BatchTiles tl = tiles[lo];
+      const uint32_t t = b - tl.base;
+      const uint3 gdim = make_uint3(tl.gx, tl.gy, tl.gz);
+      const uint3 bid = make_uint3(t % tl.gx, (t / tl.gx) % tl.gy, t / (tl.gx * tl.gy));
+      const StepArgs& a = args[lo];
+      const OfsCalc ofs{(uint32_t)a.np};
+      ForceSlot* slots = a.slots + (size_t)(pending0 + k) * a.nslots;
+      if (gather) step_tile<St, true, false, OfsCalc, false, true>(a, ofs, slots, bid, gdim);
+      else if (fields) step_tile<St, false, true, OfsCalc, false, true>(a, ofs, slots, bid, gdim);
+      else step_tile<St, false, false, OfsCalc, false, true>(a, ofs, slots, bid, gdim);
+    }
+    if (k + 1 < nsteps && !grid_barrier(sync, (k + 1) * gridDim.x)) return;
+  }
 }
 
 // Canonical initial state (LBM_INIT, wgsl.ts:147-155): f*_j = feq_j(1, (u_in,0,0))
@@ -1011,6 +1093,24 @@ cudaError_t launch_batch_t(bool gather, bool fields, dim3 block, uint32_t total_
   return launch_chained(batch_step_kernel<St, false, false>, grid, block, s, args, tiles, count, pending);
 }
 
+template <class St>
+cudaError_t launch_batch_persist_t(dim3 block, uint32_t grid, uint32_t total, const StepArgs* args,
+                                   const BatchTiles* tiles, uint32_t count, uint32_t k0, uint32_t nsteps,
+                                   uint32_t pending0, bool fields_last, unsigned int* sync, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, batch_persist_kernel<St>, args, tiles, count, total, k0, nsteps, pending0,
+                            fields_last ? 1u : 0u, sync);
+}
+
 // Host copy of feq(i, 1, (u, 0, 0)) with the reference's operation order
 // (wgsl.ts:135-138); host float arithmetic without contraction gives the same
 // bits as the device.
@@ -1096,6 +1196,29 @@ cudaError_t launch_batch_step(uint32_t storage, bool gather, bool write_fields, 
                               cudaStream_t s) {
   return by_storage(storage, [&](auto st) {
     return launch_batch_t<decltype(st)>(gather, write_fields, block, total_blocks, args, tiles, count, pending, s);
+  });
+}
+
+uint32_t batch_persist_blocks(uint32_t storage, dim3 block, uint32_t sm_count) {
+  int per_sm = 0;
+  const int threads = (int)(block.x * block.y);
+  cudaError_t e = by_storage(storage, [&](auto st) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persist_kernel<decltype(st)>, threads, 0);
+  });
+  if (e != cudaSuccess || per_sm <= 0) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (uint32_t)per_sm * sm_count;
+}
+
+cudaError_t launch_batch_persist(uint32_t storage, dim3 block, uint32_t grid, uint32_t total_blocks,
+                                 const StepArgs* args, const BatchTiles* tiles, uint32_t count, uint32_t k0,
+                                 uint32_t nsteps, uint32_t pending0, bool fields_last, unsigned int* sync,
+                                 cudaStream_t s) {
+  return by_storage(storage, [&](auto st) {
+    return launch_batch_persist_t<decltype(st)>(block, grid, total_blocks, args, tiles, count, k0, nsteps, pending0,
+                                                fields_last, sync, s);
   });
 }
 

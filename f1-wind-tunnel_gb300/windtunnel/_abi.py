@@ -198,6 +198,7 @@ _PROTOS = {
     "wt_batch_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
     "wt_batch_tune": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "wt_batch_stream": (_vp, [_vp]),
+    "wt_batch_persistent_grid": (ctypes.c_uint32, [_vp]),
     "wt_batch_last_error": (ctypes.c_char_p, [_vp]),
     "wt_version": (ctypes.c_char_p, []),
     "wt_read_coarse": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),

@@ -416,8 +416,9 @@ class AeroEngine:
 
 
 class AeroBatch:
-    """Many lattices advanced together by one kernel launch per step (the
-    aero-map sweep of src/ui/aeromap.ts:73-114 run as concurrent cases).
+    """Many lattices advanced together by one kernel launch per step, or by one
+    persistent launch per up to 64 steps (the aero-map sweep of
+    src/ui/aeromap.ts:73-114 run as concurrent cases).
     `lattices[i]` is an AeroEngine view of lattice i for voxelize/read calls."""
 
     def __init__(self, grids, sim=None, lib=None):
@@ -457,6 +458,10 @@ class AeroBatch:
 
     def stream(self):
         return self.lib.wt_batch_stream(self.b)
+
+    def persistent_grid(self):
+        """Blocks of the persistent launch, or 0 when the batch launches once per step."""
+        return self.lib.wt_batch_persistent_grid(self.b)
 
     def close(self):
         if getattr(self, "b", None):

@@ -502,8 +502,17 @@ uint32_t wt_batch_count(const wt_batch* batch);
 wt_ctx* wt_batch_lattice(wt_batch* batch, uint32_t index);
 /* n_lbm_steps / heat_passes / heat_dt as wt_step, for every lattice. */
 int wt_batch_step(wt_batch* batch, int n_lbm_steps, int heat_passes, float heat_dt);
-/* Autotuner over the block shapes for the whole batch (state saved and restored). */
+/* Autotuner over the block shapes for the whole batch, each timed with one
+ * launch per LBM step and with the persistent launch (state saved and
+ * restored).  The environment variable WT_BATCH_PERSIST=0/1, read at
+ * wt_batch_create, fixes the launch kind instead. */
 int wt_batch_tune(wt_batch* batch, uint32_t* bx, uint32_t* by, float* ms_per_step);
+/* Grid of the batch's persistent launch (blocks resident at once), or 0 when the
+ * batch launches its kernel once per LBM step.  In the persistent launch, one
+ * cooperative kernel advances every lattice by up to 64 steps (the force-record
+ * capacity), with a grid barrier between steps; the barrier's wait is bounded,
+ * and an expired wait is reported as WT_ERR_CUDA by the next wt_batch_step. */
+uint32_t wt_batch_persistent_grid(const wt_batch* batch);
 void* wt_batch_stream(wt_batch* batch);
 const char* wt_batch_last_error(const wt_batch* batch);
 
