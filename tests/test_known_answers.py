@@ -7,7 +7,13 @@ the oracle (the GPU twin is tests/test_gpu_known_answers.py):
 * momentum exchange on a single solid cell in uniform flow after one step is
   the analytic 2 rho u (wgsl.ts:221-223: every one of the 18 fluid neighbours
   bounces feq_opp(i) back and records -2 (v - w_i) c_i, which sums to
-  2 sum_j (feq_j - w_j) c_j = 2 rho u), with no lift or side force.
+  2 sum_j (feq_j - w_j) c_j = 2 rho u), with no lift or side force;
+* mass is conserved in a closed box: solid walls on every face but the
+  symmetry plane z = 0 (half-way bounce-back returns each population to its
+  cell; the mirror reflects it into one cell), a solid block inside.  The FP64
+  oracle holds the fluid mass to round-off; the reference's FP32 arithmetic
+  gains mass by the float weights' excess, 1/3, 1/18 and 1/36 as f32 literals
+  (wgsl.ts:133) summing to 1 + 1.49e-8, each step.
 """
 import numpy as np
 
@@ -45,6 +51,50 @@ def test_uniform_flow_is_a_fixed_point(oracle_mod):
     np.testing.assert_allclose(d["fields"][:, 0], U_IN, atol=2e-6)
     np.testing.assert_allclose(d["fields"][:, 1:3], 0.0, atol=2e-6)
     np.testing.assert_allclose(d["fields"][:, 3], 1.0, atol=2e-6)
+
+
+W_EXCESS = float(np.float64(np.float32(0.33333334)) + 6 * np.float64(np.float32(0.055555556))
+                 + 12 * np.float64(np.float32(0.027777778)) - 1.0)   # 1.49e-8
+BOX_DIMS = (48, 20, 16)
+BOX_U = 0.05
+
+
+def closed_box(dims=BOX_DIMS):
+    """Solid flags (u32) of the closed box: walls at x = 0, nx-1, y = 0, ny-1,
+    z = nz-1 and a block in the flow; z = 0 stays the symmetry plane."""
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    i = np.arange(n)
+    x, y, z = i % nx, (i // nx) % ny, i // (nx * ny)
+    solid = ((x == 0) | (x == nx - 1) | (y == 0) | (y == ny - 1) | (z == nz - 1)).astype(np.uint32)
+    solid[(x >= 18) & (x < 24) & (y >= 6) & (y < 12) & (z < 5)] = 2
+    return solid, np.zeros(n, np.float32)
+
+
+def test_closed_box_conserves_mass(oracle_mod):
+    from windtunnel.engine import make_sim
+    solid, emit = closed_box()
+    fluid = solid == 0
+    sim = make_sim(u_in=BOX_U, tau0=0.52, smag=0.15)
+    o64 = oracle_mod.Oracle(BOX_DIMS, (0, 0, 0), 0.1, sim, fp64=True)
+    o64.set_solid(solid, emit)
+    o64.reset()
+    m0 = o64.read64()[0][fluid, 3].sum()
+    o64.steps(2400)
+    m = o64.read64()[0][fluid, 3].sum()
+    assert abs(m - m0) <= 1e-12 * m0
+    o32 = oracle_mod.Oracle(BOX_DIMS, (0, 0, 0), 0.1, sim)
+    o32.set_solid(solid, emit)
+    o32.reset()
+    o32.steps(2)
+    m2 = o32.read()["fields"][fluid, 3].astype(np.float64).sum()
+    o32.steps(2398)
+    d = o32.read()
+    m = d["fields"][fluid, 3].astype(np.float64).sum()
+    drift = (m - m2) / m2
+    print(f"\nFP32 mass drift over 2398 steps {drift:.3e}, weights' excess x steps {2398 * W_EXCESS:.3e}")
+    assert 0.5 * 2398 * W_EXCESS <= drift <= 1.5 * 2398 * W_EXCESS
+    assert o32.guarded() == 0 and np.abs(d["fields"][fluid, :3]).max() < BOX_U
 
 
 def test_single_cell_momentum_exchange(oracle_mod):
