@@ -736,13 +736,15 @@ cudaError_t launch_chained(K kernel, dim3 grid, dim3 block, cudaStream_t s, Args
 template <class St, bool GATHER, bool FIELDS>
 __global__ void __maxnreg__(St::max_regs) step_kernel(StepArgs a) {
   chain_enter();
-  // Local steps take the tiles in reverse launch order: their first tiles are the
-  // ones the preceding gather step ran last, whose lines are still in the L2
-  // (the FP32 lattice at 256x96x80, 157 MB of populations, is larger than the
-  // L2).  Force and mass records are keyed by tile coordinates, not by launch
-  // order, so the results do not change.
+  // FP32 local steps take the tiles in reverse launch order: their first tiles
+  // are the ones the preceding gather step ran last, whose lines are still in
+  // the L2 (the FP32 lattice at 256x96x80, 157 MB of populations, is larger than
+  // the L2): +2.7 % there, neutral at 512x192x160.  For f16/bf16 it measured 9 %
+  // slower at 256x96x80 (whose populations fit the L2) and neutral at
+  // 512x192x160, so they keep the launch order.  Force and mass records are
+  // keyed by tile coordinates, not by launch order, so the results do not change.
   const uint3 gdim = make_uint3(gridDim.x, gridDim.y, gridDim.z);
-  if constexpr (GATHER) {
+  if constexpr (GATHER || St::id != WT_STORE_F32) {
     step_tile<St, GATHER, FIELDS, OfsTable, false>(a, OfsTable{a}, a.slots, blockIdx, gdim);
   } else {
     const uint3 bid = make_uint3(gdim.x - 1 - blockIdx.x, gdim.y - 1 - blockIdx.y, gdim.z - 1 - blockIdx.z);
