@@ -29,11 +29,13 @@
 // device current) on the first call on that device, and kept for the process:
 // this assumes the device's primary context lives as long as the process (no
 // cudaDeviceReset between calls).  Every call overwrites all the records it
-// reads, so nothing has to be cleared; the array is shared by all calls, so
+// reads (the guard counter it accumulates is cleared at the start of each
+// call), so nothing else has to be cleared; the array is shared by all calls, so
 // calls that overlap on the GPU (different streams, or different host threads
-// on the same device) race and must be serialised by the caller.  Each call
-// ends by synchronising its stream, so it refuses a stream that is being
-// captured.  No cudaMalloc/cudaFree or allocating library routine is called.
+// on the same device) race and must be serialised by the caller.  The first
+// call on a device does that device's set-up (the address lookup), so make it
+// before any stream capture begins.  Each call ends by synchronising its stream.
+// No cudaMalloc/cudaFree or allocating library routine is called.
 #include <string.h>
 
 #include <mutex>
@@ -249,9 +251,6 @@ extern "C" int wt_forces_noalloc(const float* f, const uint32_t* solid, const fl
   const uint64_t n = (uint64_t)nx * ny * nz;
   if (n > WT_NOALLOC_MAX_CELLS) return WT_ERR_NOALLOC_LIMIT;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return WT_ERR_CUDA;
-  if (cap != cudaStreamCaptureStatusNone) return WT_ERR_ARG;  // the call synchronises its stream
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 64) return WT_ERR_DEVICE;

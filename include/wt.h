@@ -540,15 +540,16 @@ const char* wt_version(void);
  *           trip the divergence guard contribute nothing (their count is in
  *           out->guarded); out->steps = 1, out->mass = 0.
  * Scratch is a static device array of WT_NOALLOC_BLOCKS + 2 records
- * (98,496 B) that every GPU loading the library holds until exit.  Its device
- * address is looked up on the first call on each device and kept for the
- * process, which assumes the device's primary context is not reset
- * (cudaDeviceReset) between calls.  All calls share the array: calls that
- * overlap on the GPU race.  Every call synchronises `stream` (a cudaStream_t,
- * NULL = legacy default stream) before returning, so it cannot be recorded
- * into a CUDA graph: a stream under capture is refused with WT_ERR_ARG.
- * Lattices above WT_NOALLOC_MAX_CELLS cells are rejected with
- * WT_ERR_NOALLOC_LIMIT, lattices below 8x3x3 with WT_ERR_ARG. */
+ * (98,496 B) that every GPU loading the library holds until exit.  The first
+ * call on each device does that device's set-up: it looks up the array's
+ * device address (with the device current) and keeps it for the process, which
+ * assumes the device's primary context is not reset (cudaDeviceReset) between
+ * calls.  Make that first call before any stream capture begins.  All calls
+ * share the array and each keeps the previous call's contents except what it
+ * clears: calls that overlap on the GPU race.  Every call synchronises `stream`
+ * (a cudaStream_t, NULL = legacy default stream) before returning.  Lattices
+ * above WT_NOALLOC_MAX_CELLS cells are rejected with WT_ERR_NOALLOC_LIMIT,
+ * lattices below 8x3x3 with WT_ERR_ARG. */
 #define WT_NOALLOC_BLOCKS 1024u
 #define WT_NOALLOC_MAX_CELLS 134217728ull /* 2^27 */
 #define WT_ERR_NOALLOC_LIMIT (-7)
