@@ -815,11 +815,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* sync, uint32_t target
 
 // (FP32: 8 registers above the step kernel's cap, 112 B of spills instead of 296)
 template <class St>
-__global__ void __maxnreg__(St::max_regs + (St::id == WT_STORE_F32 ? 8 : 0)) batch_persist_kernel(const StepArgs* __restrict__ args,
-                                                               const BatchTiles* __restrict__ tiles, uint32_t count,
-                                                               uint32_t total, uint32_t k0, uint32_t nsteps,
-                                                               uint32_t pending0, uint32_t fields_last,
-                                                               unsigned int* sync) {
+__global__ void __maxnreg__(St::max_regs + (St::id == WT_STORE_F32 ? 8 : 0))
+    batch_persist_kernel(const StepArgs* __restrict__ args, const BatchTiles* __restrict__ tiles, uint32_t count,
+                         uint32_t total, uint32_t k0, uint32_t nsteps, uint32_t pending0, uint32_t fields_last,
+                         unsigned int* sync) {
   for (uint32_t k = 0; k < nsteps; k++) {
     const bool gather = ((k0 + k) & 1u) == 0u;
     const bool fields = fields_last && k + 1 == nsteps;
