@@ -259,7 +259,7 @@ int set_geometry(wt_ctx* c, uint32_t bx, uint32_t by) {
   c->block_slot = nullptr;
   c->mass_partial = nullptr;
   c->geom = g;
-  c->prefetch_ahead = step_resident_blocks(c->sim.storage, g, c->sm_count);
+  c->prefetch_ahead = step_resident_blocks(c->sim.storage, g, c->sm_count, 19ull * c->np * c->elem, c->l2_bytes);
   c->bx = g.block.x;
   c->by = g.block.y;
   int rc;
@@ -308,7 +308,8 @@ int create_ctx(const wt_grid* grid, const wt_sim* sim, cudaStream_t ext, wt_ctx*
   if (const char* s = getenv("WT_STEP_BX")) c->bx = (uint32_t)atoi(s);
   if (const char* s = getenv("WT_STEP_BY")) c->by = (uint32_t)atoi(s);
   c->geom = step_geometry(c->nx, c->ny, c->nz, c->bx, c->by);
-  c->prefetch_ahead = step_resident_blocks(c->sim.storage, c->geom, c->sm_count);
+  c->l2_bytes = (uint64_t)prop.l2CacheSize;
+  c->prefetch_ahead = step_resident_blocks(c->sim.storage, c->geom, c->sm_count, 19ull * np * c->elem, c->l2_bytes);
   c->bx = c->geom.block.x;
   c->by = c->geom.block.y;
   int rc = 0;

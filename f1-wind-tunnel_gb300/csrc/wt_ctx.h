@@ -29,6 +29,7 @@ struct wt_ctx {
   size_t elem = 4;
   wt::StepGeom geom{};
   uint32_t sm_count = 0;
+  uint64_t l2_bytes = 0;        // the device's L2 size
   uint32_t prefetch_ahead = 0;  // resident step blocks at the current block shape
   // device buffers
   void* pop = nullptr;

@@ -87,8 +87,11 @@ struct StepGeom {
 };
 
 StepGeom step_geometry(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx, uint32_t by);
-// Blocks of the collide-stream kernel resident on the whole device at this block shape.
-uint32_t step_resident_blocks(uint32_t storage, const StepGeom& g, uint32_t sm_count);
+// Blocks of the collide-stream kernel resident on the whole device at this block
+// shape: the L2 prefetch distance, or 0 where the prefetch stays off (f16/bf16;
+// f32 populations within twice the L2).
+uint32_t step_resident_blocks(uint32_t storage, const StepGeom& g, uint32_t sm_count, uint64_t pop_bytes,
+                              uint64_t l2_bytes);
 
 // Block ranges of the lattices of a batch launch (see batch_step_kernel).
 struct BatchTiles {

@@ -1138,11 +1138,14 @@ cudaError_t by_storage(uint32_t storage, F&& f) {
 }  // namespace
 
 // Prefetch distance of the collide-stream kernel: one wave of resident blocks for
-// f32 storage; 0 (off) for f16/bf16, where the extra L2 traffic measured slower
-// (34.3 -> 30.4 GLUPS on the 256x96x80 F1) while f32 gained (77.5 -> 79.8 % of
-// the HBM roofline on the 512x192x160 F1).
-uint32_t step_resident_blocks(uint32_t storage, const StepGeom& g, uint32_t sm_count) {
-  if (storage != WT_STORE_F32) return 0;
+// f32 storage whose populations exceed twice the L2; 0 (off) otherwise.  f16/bf16
+// measured slower with it (34.3 -> 30.4 GLUPS on the 256x96x80 F1); f32 gained at
+// 512x192x160 (77.5 -> 79.8 % of the HBM roofline, 1.2 GB of populations) but at
+// 256x96x80 (150 MB, with the alternating sweep order reusing the L2) it evicts
+// lines the next step reads: kernel 32.8 GLUPS with it, 35.0 without.
+uint32_t step_resident_blocks(uint32_t storage, const StepGeom& g, uint32_t sm_count, uint64_t pop_bytes,
+                              uint64_t l2_bytes) {
+  if (storage != WT_STORE_F32 || pop_bytes <= 2 * l2_bytes) return 0;
   int per_sm = 0;
   const int threads = (int)(g.block.x * g.block.y);
   cudaError_t e = by_storage(storage, [&](auto st) {
