@@ -13,7 +13,11 @@ the oracle (the GPU twin is tests/test_gpu_known_answers.py):
   cell; the mirror reflects it into one cell), a solid block inside.  The FP64
   oracle holds the fluid mass to round-off; the reference's FP32 arithmetic
   gains mass by the float weights' excess, 1/3, 1/18 and 1/36 as f32 literals
-  (wgsl.ts:133) summing to 1 + 1.49e-8, each step.
+  (wgsl.ts:133) summing to 1 + 1.49e-8, each step;
+* the heat pass (wgsl.ts:460-511) on a temperature field linear in x, in
+  uniform flow without sources: the trilinear backtrace of a linear field and
+  the mean of its six neighbours are exact, so each pass maps a + b x to
+  (1 - cool) (a + b x - (1 - diffuse) b u dt) away from the boundaries.
 """
 import numpy as np
 
@@ -95,6 +99,29 @@ def test_closed_box_conserves_mass(oracle_mod):
     print(f"\nFP32 mass drift over 2398 steps {drift:.3e}, weights' excess x steps {2398 * W_EXCESS:.3e}")
     assert 0.5 * 2398 * W_EXCESS <= drift <= 1.5 * 2398 * W_EXCESS
     assert o32.guarded() == 0 and np.abs(d["fields"][fluid, :3]).max() < BOX_U
+
+
+def test_heat_pass_on_a_linear_field(oracle_mod):
+    from windtunnel.engine import make_sim
+    dims = (32, 12, 10)
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    u, dt, a, b = 0.05, 4.0, 0.3, 0.01
+    sim = make_sim(u_in=u, tau0=0.52, smag=0.15)
+    o = oracle_mod.Oracle(dims, (0, 0, 0), 0.1, sim)
+    o.set_solid(np.zeros(n, np.uint32), np.zeros(n, np.float32))
+    o.reset()
+    x = (np.arange(n) % nx).astype(np.float64)
+    fields = np.zeros((n, 4), np.float32)
+    fields[:, 0], fields[:, 3] = u, 1.0
+    o.write_state(fields=fields, temps=(a + b * x).astype(np.float32))
+    o.heat(dt)  # the frame's two passes
+    got = o.read()["temps"].astype(np.float64)
+    keep = (1.0 - sim.heat_cool) ** 2
+    want = keep * (a + b * x - 2.0 * (1.0 - sim.heat_diffuse) * b * u * dt)
+    inner = (x >= 3) & (x <= nx - 4)
+    np.testing.assert_allclose(got[inner], want[inner], rtol=2e-6, atol=0)
+    assert np.all(got[x == 0] < want[x == 0])  # the inlet side mixes in the T = 0 inflow
 
 
 def test_single_cell_momentum_exchange(oracle_mod):
